@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 MEMD engine on the 32-channel EEG-shaped workload.
+
+Workload (one "step" = one full decomposition): 32 channels x 30,504 samples
+(fs = 256 Hz, seeded EEG-shaped synthetic record), 128 Hammersley directions,
+9 output slots = 8 IMFs x 10 sifts + residual (the reference's fixed mode,
+memReducedEpochs_dev.cu:1473-1476), i.e. 80 sifts per step.
+
+Metric: channel-samples/s = C*L / (device time of one decomposition), for
+the precision form that meets <= 1e-4 relative L2 per IMF against the FP64
+path (FP32 form when it meets the gate, else FP64); sift iterations/s beside
+it.  Inputs resident in HBM for `value`; `e2e` adds the pinned host->device
+copy of the record and the device->host copy of all IMFs through the C ABI.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank decomposes its own record (a replica with
+its own seed, no exchange): weak scaling, max time over ranks.
+--impl reference times the reference algorithm's CPU transcription (the FP64
+OpenMP oracle, all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "memd-gpu_gb300", "py"))
+
+METRIC = "channel-samples/sec at ≤1e-4 rel-L2 per IMF vs FP64 (1 GB300); sift iters/sec"
+WL = dict(workload="eeg32_30504_k128_fixed", C=32, L=30504, K=128, num_imfs=9, max_iter=10, fs=256.0)
+SIFTS = (WL["num_imfs"] - 1) * WL["max_iter"]
+GATE = 1e-4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ----------------------------------------------------------------------------
+# clocks sampling (nvidia-smi during the timed region)
+# ----------------------------------------------------------------------------
+SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class Clocks:
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={SMI_FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.f.read())) if len(r) >= 9]
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------
+# algorithmic work per stage (flops, bytes) from the knot counts of a traced run
+# ----------------------------------------------------------------------------
+def stage_work(C, L, K, sifts, sum_E, rb):
+    """sum_E: total knots over all sifts, directions and both envelopes."""
+    KCL = float(K) * C * L * sifts
+    CE = float(C) * sum_E
+    return {
+        # P = dir . X: one fma per (direction, channel, sample)
+        "project": {"flops": 2.0 * KCL, "bytes": sifts * (C * L * rb + 2.0 * K * L / 8.0)},
+        "compact": {"flops": 0.0, "bytes": sifts * 2.0 * K * L / 8.0 + 4.0 * sum_E},
+        "factor": {"flops": 8.0 * sum_E, "bytes": sum_E * (4.0 + 4 * rb)},
+        # slope, rhs, forward (2), backward (1) per knot and channel
+        "solve": {"flops": 7.0 * CE, "bytes": CE * (rb + 3 * 2 * rb) + sum_E * 4 * rb},
+        # per sample, channel, direction: 2 envelopes x 3 fma + 2 adds;
+        # per knot and channel: 9 flops of coefficients
+        "eval": {"flops": 14.0 * KCL + 9.0 * CE, "bytes": 2.0 * rb * CE + sifts * 2.0 * C * L * rb},
+    }
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def load_profile_traffic():
+    """Per-launch DRAM bytes of the dominant kernels from the committed ncu
+    summary (profiles/ncu_traffic.json), if present."""
+    p = os.path.join(REPO, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return {}
+    return {}
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import memd_gb300 as mg
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+    C, L, K, NI, IT = WL["C"], WL["L"], WL["K"], WL["num_imfs"], WL["max_iter"]
+    y = mg.synth_eeg(C, L, WL["fs"], seed=rank)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    results = {}
+    outs = {}
+    plans = {}
+    for name, prec, tdt, dname in (("fp64", mg.PREC_F64, torch.float64, "f64"),
+                                   ("fp32", mg.PREC_F32, torch.float32, "f32")):
+        plan = mg.Plan(C, L, K, NI, IT, precision=prec)
+        plans[name] = plan
+        d = mg.directions(C, K, dtype=dname)
+        dy = torch.as_tensor(y, dtype=tdt, device="cuda")
+        out = torch.empty((NI, C, L), dtype=tdt, device="cuda")
+        for _ in range(args.warmup):
+            plan.run(dy, d, out, stream=stream, stats=False)
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks = Clocks(local) if rank == 0 else None
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (256 MB > 129 MB L2)
+            ev[i][0].record(stream)
+            plan.run(dy, d, out, stream=stream, stats=False)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ck = clocks.stop() if clocks else None
+        ms = [a.elapsed_time(b) for a, b in ev]
+        tot = torch.tensor([sum(ms)], dtype=torch.float64, device="cuda")
+        if ws > 1:
+            dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+        st = plan.run(dy, d, out, stats=True)
+        results[name] = {"ms_per_step": float(tot.item()) / args.steps, "wall_s": wall, "clocks": ck,
+                         "launches_per_step": int(st.launches), "flags": int(st.flags),
+                         "workspace_gb": plan.workspace_bytes / 1e9}
+        outs[name] = (out, d, dy)
+
+    # precision gate: FP32 form against the FP64 path, per IMF
+    ref = outs["fp64"][0].cpu().numpy()
+    f32 = outs["fp32"][0].cpu().numpy()
+    rl = [rel_l2(f32[i], ref[i]) for i in range(NI)]
+    gate_ok = all(r <= GATE for r in rl)
+    head = "fp32" if gate_ok else "fp64"
+
+    # e2e through the C ABI with host buffers (pinned), headline precision
+    plan = plans[head]
+    tdt = torch.float32 if head == "fp32" else torch.float64
+    hy = torch.as_tensor(y, dtype=tdt).pin_memory()
+    hout = torch.empty((NI, C, L), dtype=tdt).pin_memory()
+    dy = torch.empty((C, L), dtype=tdt, device="cuda")
+    dout = torch.empty((NI, C, L), dtype=tdt, device="cuda")
+    d = outs[head][1]
+    for _ in range(2):
+        dy.copy_(hy, non_blocking=True)
+        plan.run(dy, d, dout, stream=stream, stats=False)
+        hout.copy_(dout, non_blocking=True)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        dy.copy_(hy, non_blocking=True)
+        plan.run(dy, d, dout, stream=stream, stats=False)
+        hout.copy_(dout, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = torch.tensor([e0.elapsed_time(e1) / args.steps], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        dist.all_reduce(e2e_ms, op=dist.ReduceOp.MAX)
+    e2e_ms = float(e2e_ms.item())
+    elem = 4 if head == "fp32" else 8
+
+    # per-stage timing (eager, every kernel bracketed by CUDA events) and knot
+    # counts (traced run) for the roofline of the dominant kernel
+    stage = {}
+    for name in ("fp64", "fp32"):
+        p = plans[name]
+        out, dd, yy = outs[name]
+        prof = p.profile(yy, dd, out).as_dict()
+        p.set_trace(True)
+        p.run(yy, dd, out)
+        tr = p.trace()
+        p.set_trace(False)
+        sum_E = float(tr["count"][: NI - 1, :IT].astype(np.int64).sum())
+        rb = 8 if name == "fp64" else 4
+        work = stage_work(C, L, K, SIFTS, sum_E, rb)
+        stage[name] = {"profile": prof, "sum_knots": sum_E, "work": work}
+
+    meas = {}
+    peaks_path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        meas = json.load(open(peaks_path))
+    hbm_peak = meas.get("hbm_gbs", 6800.0)
+    traffic = load_profile_traffic()
+
+    def roofline(name):
+        prof = stage[name]["profile"]
+        work = stage[name]["work"]
+        dom = max(("project", "compact", "factor", "solve", "eval"), key=lambda s: prof[s]["ms"])
+        ms = prof[dom]["ms"]
+        n = max(prof[dom]["launches"], 1)
+        per_launch_s = ms / 1e3 / n
+        b = work[dom]["bytes"] / n
+        f = work[dom]["flops"] / n
+        tr = traffic.get(f"{name}:{dom}")
+        out = {"kernel": dom, "bound": "hbm", "achieved": b / per_launch_s / 1e9, "peak": hbm_peak,
+               "unit": "GB/s", "frac": (b / per_launch_s / 1e9) / hbm_peak,
+               "traffic": tr.get("bytes_per_launch") if tr else None,
+               "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if meas else "fallback 6.8 TB/s",
+               "alg_bytes_per_launch": b, "alg_flops_per_launch": f, "avg_launch_ms": ms / n, "launches": n,
+               "achieved_tflops": f / per_launch_s / 1e12,
+               "stage_ms": {s: round(prof[s]["ms"], 3) for s in prof}}
+        return out
+
+    line = None
+    if rank == 0:
+        hv = results[head]
+        value = ws * C * L / (hv["ms_per_step"] / 1e3)
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "channel-samples/s",
+            "n_gpus": ws,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": hv["ms_per_step"],
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32" if head == "fp32" else "f64",
+            "data": "synthetic EEG-shaped (seeded 1/f mixture + alpha bursts + drift), generated on the host",
+            "config": {"workload": WL["workload"], "C": C, "L": L, "K": K, "num_imfs": NI, "max_iter": IT,
+                       "sifts_per_step": SIFTS, "mode": "fixed (reference)", "l2": "flushed between steps",
+                       "parallelism": "replicas" if ws > 1 else "single"},
+            "sift_iters_per_s": ws * SIFTS / (hv["ms_per_step"] / 1e3),
+            "precision_gate": {"form": "fp32", "rel_l2_per_imf_vs_fp64": rl, "max": max(rl), "passed": gate_ok},
+            "fp64": {"ms_per_step": results["fp64"]["ms_per_step"],
+                     "channel_samples_per_s": ws * C * L / (results["fp64"]["ms_per_step"] / 1e3),
+                     "workspace_gb": results["fp64"]["workspace_gb"], "flags": results["fp64"]["flags"]},
+            "fp32": {"ms_per_step": results["fp32"]["ms_per_step"],
+                     "channel_samples_per_s": ws * C * L / (results["fp32"]["ms_per_step"] / 1e3),
+                     "workspace_gb": results["fp32"]["workspace_gb"], "flags": results["fp32"]["flags"]},
+            "e2e": {"value": ws * C * L / (e2e_ms / 1e3), "unit": "channel-samples/s",
+                    "h2d_bytes_per_step": C * L * elem, "d2h_bytes_per_step": NI * C * L * elem,
+                    "ms_per_step": e2e_ms, "api": "memd_run_f32/f64 (C ABI) via ctypes"},
+            "gpu_launches": results[head]["launches_per_step"] * args.steps,
+            "roofline": roofline(head),
+            "roofline_fp64_path": roofline("fp64"),
+            "clocks": results[head]["clocks"],
+        }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(y, outs["fp64"][1].cpu().numpy())
+    if rank == 0 and not args.no_reference_gpu:
+        line["reference_gpu"] = reference_gpu(y)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    for p in plans.values():
+        p.close()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline: the FP64 OpenMP oracle (a transcription of the reference
+# algorithm) on a bounded sample: all 8 IMF stages with one sift each, scaled
+# to the 80 sifts of the full decomposition.
+# ----------------------------------------------------------------------------
+def cpu_baseline(y, dirs, reps: int = 1):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    C, L = y.shape
+    NI = WL["num_imfs"]
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.memd(y, dirs, NI, 1)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    sample_sifts = NI - 1
+    full_s = best * SIFTS / sample_sifts
+    return {"value": C * L / full_s, "unit": "channel-samples/s", "cores": oracle.max_threads(),
+            "kind": "port", "sample": f"full record, {sample_sifts} of {SIFTS} sifts (1 per IMF stage), "
+                                     f"{best:.2f} s, scaled x{SIFTS / sample_sifts:.0f}",
+            "nproc": os.cpu_count()}
+
+
+# ----------------------------------------------------------------------------
+# the reference's own CUDA build (oracle/_ref, FP32 as shipped) on this GPU
+# ----------------------------------------------------------------------------
+def reference_gpu(y, repeats: int = 3):
+    exe = os.path.join(REPO, "oracle", "_ref", "memd_ref_f32")
+    if not os.path.exists(exe):
+        return {"unavailable": "reference build not present (oracle/_ref)"}
+    C, L = y.shape
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.bin")
+        y.astype(np.float32).tofile(inp)
+        cmd = [exe, inp, str(C), str(WL["K"]), str(WL["num_imfs"]), str(WL["max_iter"]),
+               os.path.join(td, "out.bin"), "-", str(repeats)]
+        p = subprocess.run(cmd, capture_output=True, text=True, timeout=1200)
+    try:
+        r = json.loads(p.stdout.strip().splitlines()[-1])
+    except Exception:
+        return {"unavailable": f"reference run failed rc={p.returncode}: {p.stderr[-300:]}"}
+    if "unavailable" in r:
+        return r
+    return {"precision": "f32 (as shipped)", "best_call_ms": r["best_call_ms"], "best_loop_s": r["best_loop_s"],
+            "channel_samples_per_s_call": C * L / (r["best_call_ms"] / 1e3),
+            "channel_samples_per_s_loop": C * L / r["best_loop_s"], "repeats": repeats,
+            "note": "call = cudaEvents around memd() incl. its workspace allocation; loop = its own omp_get_wtime"}
+
+
+# ----------------------------------------------------------------------------
+# reference arm: the CPU transcription of the reference algorithm
+# ----------------------------------------------------------------------------
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import memd_gb300 as mg
+    import oracle
+
+    C, L, K, NI = WL["C"], WL["L"], WL["K"], WL["num_imfs"]
+    y = mg.synth_eeg(C, L, WL["fs"], seed=0)
+    dirs = oracle.directions(C, K)
+    sample_sifts = NI - 1
+    for _ in range(args.warmup):
+        oracle.memd(y, dirs, NI, 1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.memd(y, dirs, NI, 1)
+        times.append(time.perf_counter() - t0)
+    per_step_full = float(np.mean(times)) * SIFTS / sample_sifts
+    value = C * L / per_step_full
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "channel-samples/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": per_step_full * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic EEG-shaped (seeded), same record as the GPU arm",
+        "config": {"workload": WL["workload"], "C": C, "L": L, "K": K, "num_imfs": NI,
+                   "max_iter": WL["max_iter"], "sifts_per_step": SIFTS, "mode": "fixed (reference)"},
+        "cpu_baseline": {"value": value, "unit": "channel-samples/s", "cores": oracle.max_threads(),
+                         "kind": "port",
+                         "sample": f"each step: {sample_sifts} of {SIFTS} sifts (1 per IMF stage) of the full "
+                                   f"record, scaled x{SIFTS / sample_sifts:.0f}"},
+        "e2e": {"value": value, "unit": "channel-samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference implements this path only as CUDA (no CPU code); its CPU arm is the FP64 OpenMP "
+                "transcription (oracle/), timed on all host threads",
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

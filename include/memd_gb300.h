@@ -1,0 +1,192 @@
+/*
+ * memd_gb300.h -- C ABI of the GB300 MEMD engine (libmemd_gb300.so).
+ *
+ * Multivariate empirical mode decomposition (Rehman & Mandic 2010) of a
+ * C-channel record of L samples with K projection directions, on one GPU.
+ * The entry points replace the reference's host interface for this path
+ * (reference files memReducedEpochs_dev.cu and memdMatlabCuda.cu):
+ *
+ *   memd_plan_create / memd_run_f64 / memd_run_f32 / memd_plan_destroy
+ *       replace  template<coord_t, real_t> double memd(size_t SignalDim,
+ *                size_t SignalLength, size_t NumDirVector, size_t num_IMFs,
+ *                size_t max_iter, coord_t* d_x, real_t* d_y,
+ *                real_t* d_DirectionVectors, real_t* d_IMFs)
+ *                memReducedEpochs_dev.cu:1074-1368, which allocates and frees
+ *                its workspace on every call; here the workspace belongs to
+ *                the plan and a run allocates nothing.
+ *   memd_directions_f64 / memd_directions_f32
+ *       replace  template<T> void GenerateDirectionVector(size_t SignalDim,
+ *                size_t NumDirVector, T* d_DirectionVector)
+ *                memReducedEpochs_dev.cu:1029-1072 (primes == NULL), and the
+ *                in-line direction set of the MEX entry
+ *                memdMatlabCuda.cu:1131-1152 (primes = the caller's table).
+ *   memd_run_batched_f64 / memd_run_batched_f32
+ *       no single reference counterpart: the reference decomposes one record
+ *       per memd() call (runBenchmark, memReducedEpochs_dev.cu:1370-1464,
+ *       loops over calls); this decomposes many records of equal C and
+ *       uneven L in one pass.
+ *
+ * Data layout (identical to the reference):
+ *   d_y     C x L, channel-major (y[c*L + n])
+ *   d_dir   K x C, direction-major (dir[k*C + c])
+ *   d_imfs  num_imfs x C x L; slot i < num_imfs-1 is IMF i, the last slot
+ *           holds the residual.
+ *   d_x     the sample coordinate 0..L-1 (int32); the reference compares the
+ *           sample index with these values (memReducedEpochs_dev.cu:812-826),
+ *           so any other content is rejected (MEMD_ERR_COORD) when d_x is
+ *           given; pass NULL to skip the check.
+ *
+ * All calls are stream-ordered on the given stream (cudaStream_t passed as
+ * void*, NULL = legacy default stream) and return a memd_status.  A plan is
+ * not thread-safe: one run at a time per plan.
+ */
+#ifndef MEMD_GB300_H
+#define MEMD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MEMD_OK = 0,
+    MEMD_ERR_INVALID = 1,      /* bad size / argument / null pointer */
+    MEMD_ERR_CUDA = 2,         /* a CUDA runtime call failed; see memd_last_error() */
+    MEMD_ERR_NOMEM = 3,        /* device or host allocation failed at plan creation */
+    MEMD_ERR_COORD = 4,        /* d_x is not 0..L-1 */
+    MEMD_ERR_PRECISION = 5,    /* run_f64 on a plan built for f32 or the reverse */
+    MEMD_ERR_UNSUPPORTED = 6   /* combination not built (e.g. stop mode + batched) */
+} memd_status;
+
+typedef enum {
+    MEMD_PREC_F64 = 0,     /* plain FP64 end to end (the drop-in / parity path) */
+    MEMD_PREC_F32 = 1,     /* FP32 end to end (the reference's own precision) */
+    MEMD_PREC_MIXED = 2    /* FP32 storage and splines, FP64 where it matters */
+} memd_precision;
+
+typedef enum {
+    MEMD_STOP_FIXED = 0,   /* exactly max_iter sifts per IMF (the reference) */
+    MEMD_STOP_CRITERION = 1/* Rilling et al. 2003 thresholds (sd, sd2, tol) */
+} memd_stop_mode;
+
+typedef struct {
+    int64_t channels;      /* C >= 1 */
+    int64_t length;        /* L >= 4 (batched: maximum epoch length) */
+    int64_t directions;    /* K >= 1 */
+    int64_t num_imfs;      /* output slots >= 1 (IMFs + residual) */
+    int64_t max_iter;      /* sifts per IMF (fixed) or cap (criterion) */
+    int32_t precision;     /* memd_precision */
+    int32_t stop_mode;     /* memd_stop_mode */
+    double stop_sd;        /* theta1, default 0.075 */
+    double stop_sd2;       /* theta2, default 0.75 */
+    double stop_tol;       /* alpha, default 0.075 */
+    int32_t ref_window;    /* 1: extrema tested only at interior samples
+                              n <= 240*ceil(L/242), as the reference's launch
+                              (memReducedEpochs_dev.cu:1191-1195) does; 0: all */
+    int32_t dir_chunk;     /* directions per pass (0 = all K at once) */
+    int32_t solve_window;  /* tridiagonal halo in knots (0 = default; <0 = exact) */
+    int32_t max_epochs;    /* batched runs: epochs per call (0 = single record) */
+    int64_t reserved[4];
+} memd_config;
+
+typedef struct {
+    int32_t n_imfs;        /* IMFs extracted (excluding the residual slot) */
+    int32_t flags;         /* MEMD_FLAG_* bits seen during the run */
+    double elapsed_ms;     /* device time of the decomposition (CUDA events) */
+    int64_t launches;      /* kernels this library launched for the run */
+    int32_t sifts[64];     /* sifts per IMF (first 64 IMFs) */
+} memd_stats;
+
+/* Per-stage device time of one eagerly launched decomposition (every kernel
+ * bracketed by CUDA events on the run's stream). */
+enum {
+    MEMD_STAGE_PROJECT = 0,   /* projection + extrema bitmasks */
+    MEMD_STAGE_COMPACT = 1,   /* knot lists, counts, end-point clamp */
+    MEMD_STAGE_FACTOR = 2,    /* tridiagonal factorisation */
+    MEMD_STAGE_SOLVE = 3,     /* tridiagonal substitution */
+    MEMD_STAGE_EVAL = 4,      /* envelope evaluation + mean + update */
+    MEMD_STAGE_OTHER = 5,     /* layout transforms, IMF bookkeeping, stop tests */
+    MEMD_STAGES = 8
+};
+typedef struct {
+    double ms[MEMD_STAGES];
+    int64_t launches[MEMD_STAGES];
+} memd_profile;
+
+#define MEMD_FLAG_NO_QUALIFIED_DIRECTION 1  /* a sift had no direction with >3 maxima
+                                               and >3 minima: the reference's 0/0 NaN */
+#define MEMD_FLAG_KNOT_OVERFLOW 2           /* internal knot capacity exceeded */
+
+/* One entry per (IMF, sift, direction, envelope) when a trace buffer is
+ * given: the extrema index set of that projected direction. */
+typedef struct {
+    int32_t count;   /* knots, both end samples included */
+    int32_t flags;
+    uint64_t hash;   /* sum over the knot sample indices n of splitmix64(n), mod 2^64 */
+} memd_trace_entry;
+
+typedef struct memd_plan memd_plan;
+
+void memd_default_config(memd_config* cfg);
+
+/* Allocates every device buffer the runs need (nothing is allocated later). */
+memd_status memd_plan_create(const memd_config* cfg, memd_plan** plan);
+memd_status memd_plan_destroy(memd_plan* plan);
+/* Device bytes held by the plan. */
+size_t memd_plan_workspace_bytes(const memd_plan* plan);
+
+/* Optional per-sift trace: trace has num_imfs*(max_iter+1)*K*2 entries in
+ * [imf][sift][direction][max=0|min=1] order (host or device memory reachable
+ * by the GPU is not required: the plan copies into its own buffer and the
+ * entries are written back to this host array at the end of the run). */
+memd_status memd_plan_set_trace(memd_plan* plan, memd_trace_entry* host_trace);
+
+/* Full decomposition.  stats may be NULL; when given the call waits for the
+ * run to finish and fills it. */
+memd_status memd_run_f64(memd_plan* plan, const int32_t* d_x, const double* d_y,
+                         const double* d_dir, double* d_imfs, void* stream,
+                         memd_stats* stats);
+memd_status memd_run_f32(memd_plan* plan, const int32_t* d_x, const float* d_y,
+                         const float* d_dir, float* d_imfs, void* stream,
+                         memd_stats* stats);
+
+/* Same decomposition as memd_run_*, launched kernel by kernel without the
+ * graph, each kernel timed with CUDA events; for per-kernel roofline figures.
+ * Synchronises the stream. */
+memd_status memd_profile_f64(memd_plan* plan, const double* d_y, const double* d_dir, double* d_imfs,
+                             void* stream, memd_profile* prof);
+memd_status memd_profile_f32(memd_plan* plan, const float* d_y, const float* d_dir, float* d_imfs,
+                             void* stream, memd_profile* prof);
+
+/* Batched: n_epochs records of C channels; epoch e has length lengths[e]
+ * (host array, 4 <= lengths[e] <= cfg.length) and its samples at
+ * d_y + offsets[e] (C x lengths[e], channel-major); its IMFs go to
+ * d_imfs + num_imfs*offsets[e] (num_imfs x C x lengths[e]).  offsets is a
+ * host array of n_epochs entries in units of elements. */
+memd_status memd_run_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
+                                 const int64_t* offsets, const double* d_y, const double* d_dir,
+                                 double* d_imfs, void* stream, memd_stats* stats);
+memd_status memd_run_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
+                                 const int64_t* offsets, const float* d_y, const float* d_dir,
+                                 float* d_imfs, void* stream, memd_stats* stats);
+
+/* Direction set on the device.  primes == NULL: the standalone convention
+ * (table {-K, 2, 3, 5, ...}); otherwise primes[0..C-1] (host memory) as the
+ * MEX entry receives them.  d_dir: K x C. */
+memd_status memd_directions_f64(int64_t channels, int64_t directions, const int32_t* primes,
+                                double* d_dir, void* stream);
+memd_status memd_directions_f32(int64_t channels, int64_t directions, const int32_t* primes,
+                                float* d_dir, void* stream);
+
+/* Text of the last error on this thread. */
+const char* memd_last_error(void);
+/* Library version string. */
+const char* memd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MEMD_GB300_H */

@@ -1,0 +1,556 @@
+// memd_api.cu -- plan, workspace, CUDA-graph capture and the C ABI entry points.
+//
+// A plan owns every device buffer of the decomposition; a run copies the
+// caller's record into the plan's sample-major working layout, launches the
+// captured graph of the whole decomposition (all IMFs, all sifts, every
+// kernel of every sift: reference loop memReducedEpochs_dev.cu:1176-1338) and
+// copies the IMFs out.  Fixed-iteration runs have no data-dependent host
+// control at all, so the graph is captured once per plan and relaunched.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "memd_internal.h"
+#include "memd_kernels.cuh"
+
+namespace memd {
+
+static thread_local std::string g_err;
+
+memd_status set_error(memd_status code, const char* msg)
+{
+    g_err = msg;
+    return code;
+}
+
+memd_status set_cuda_error(const char* where, cudaError_t e)
+{
+    g_err = std::string(where) + ": " + cudaGetErrorString(e);
+    return MEMD_ERR_CUDA;
+}
+
+static int next_pow2(int v)
+{
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+}  // namespace memd
+
+using memd::Fac;
+using memd::Geom;
+using memd::RunState;
+using memd::SY;
+
+struct memd_plan {
+    memd_config cfg;
+    Geom g;
+    int real_bytes;
+    int Kc, nchunks;
+    int S, H, Sf, Hf;
+    int GS, ngroups;
+    int evalG, evalSPT, evalT;
+    size_t eval_smem, proj_smem, solve_smem;
+    void* X;
+    void* run;
+    void* dir;
+    void* acc;
+    void* imf;
+    void* yb;
+    void* fac;
+    void* sy;
+    void* rtab;
+    uint32_t* bits;
+    int* wpref;
+    int* knots;
+    int* cnt;
+    RunState* st;
+    int* coord_bad;
+    int* host_flag;
+    memd_trace_entry* trace_dev;
+    memd_trace_entry* trace_host;
+    size_t trace_n;
+    std::vector<void*> allocs;
+    size_t bytes;
+    cudaStream_t cap;
+    cudaGraphExec_t exec;
+    int64_t graph_launches;
+    cudaEvent_t e0, e1;
+};
+
+namespace memd {
+
+static memd_status dev_alloc(memd_plan* p, void** ptr, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        cudaGetLastError();
+        return set_error(MEMD_ERR_NOMEM, "plan: device allocation failed");
+    }
+    p->allocs.push_back(*ptr);
+    p->bytes += bytes;
+    return MEMD_OK;
+}
+
+// ----- eval dispatch -------------------------------------------------------
+template <typename real, int G, int SPT>
+static cudaError_t eval_attr()
+{
+    const size_t smem = EvalShape<real, G, SPT>::smem_bytes(1024);
+    return cudaFuncSetAttribute(k_eval<real, G, SPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <typename real, int G, int SPT>
+static void eval_launch(memd_plan* p, cudaStream_t s, int k0, int kc, int first, int last)
+{
+    using Sh = EvalShape<real, G, SPT>;
+    dim3 grid((unsigned)((p->g.L + Sh::T - 1) / Sh::T), (unsigned)((p->g.C + G - 1) / G));
+    k_eval<real, G, SPT><<<grid, 256, Sh::smem_bytes(p->Kc), s>>>(
+        (real*)p->X, (real*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const Fac<real>*)p->fac,
+        (const SY<real>*)p->sy, p->g, k0, kc, first, last, p->st);
+}
+
+#define MEMD_EVAL_CASES(X_)                                                                \
+    X_(4, 2) X_(4, 4) X_(4, 8) X_(8, 2) X_(8, 4) X_(8, 8) X_(16, 2) X_(16, 4) X_(16, 8) \
+    X_(32, 4) X_(32, 8)
+
+template <typename real>
+static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first, int last)
+{
+#define MEMD_CASE(G_, S_)                                         \
+    if (p->evalG == G_ && p->evalSPT == S_) {                     \
+        eval_launch<real, G_, S_>(p, s, k0, kc, first, last);     \
+        return;                                                   \
+    }
+    MEMD_EVAL_CASES(MEMD_CASE)
+#undef MEMD_CASE
+}
+
+template <typename real>
+static cudaError_t set_attrs(memd_plan* p)
+{
+    cudaError_t e = cudaSuccess;
+#define MEMD_CASE(G_, S_) \
+    if (p->evalG == G_ && p->evalSPT == S_) e = eval_attr<real, G_, S_>();
+    MEMD_EVAL_CASES(MEMD_CASE)
+#undef MEMD_CASE
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_project_extrema<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->proj_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_solve<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(p->solve_smem, 1));
+    return e;
+}
+
+// ----- launch accounting / per-stage timing --------------------------------
+// Counts every kernel launch; when a profile is requested, brackets each
+// launch with CUDA events on the launching stream and waits for it.
+struct Launches {
+    int64_t count = 0;
+    memd_profile* prof = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaStream_t s = nullptr;
+    void begin()
+    {
+        if (prof) cudaEventRecord(a, s);
+    }
+    void end(int stage)
+    {
+        ++count;
+        if (!prof) return;
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        prof->ms[stage] += ms;
+        prof->launches[stage] += 1;
+    }
+};
+
+// ----- one sift, all direction chunks ---------------------------------------
+template <typename real>
+static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, Launches& lc)
+{
+    const Geom& g = p->g;
+    for (int ch = 0; ch < p->nchunks; ++ch) {
+        const int k0 = ch * p->Kc;
+        const int kc = std::min(p->Kc, g.K - k0);
+        dim3 pg((unsigned)((g.L + kProjTN - 1) / kProjTN), (unsigned)((kc + kProjTK - 1) / kProjTK));
+        lc.begin();
+        k_project_extrema<real><<<pg, 256, p->proj_smem, s>>>((const real*)p->X, (const real*)p->dir, p->bits, g, k0, kc);
+        lc.end(MEMD_STAGE_PROJECT);
+        lc.begin();
+        k_compact<real><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (real*)p->yb,
+                                                           (const real*)p->X, trace, g, k0, kc, p->st);
+        lc.end(MEMD_STAGE_COMPACT);
+        const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
+        const long nf = 2L * kc * nsegf;
+        lc.begin();
+        k_factor<real><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const real*)p->rtab,
+                                                                    (Fac<real>*)p->fac, g, k0, kc, p->Sf, p->Hf);
+        lc.end(MEMD_STAGE_FACTOR);
+        const long nseg = (g.cap + p->S - 1) / p->S;
+        const long ns = 2L * kc * nseg * p->ngroups * p->GS;
+        lc.begin();
+        k_solve<real><<<(unsigned)((ns + kSolveThreads - 1) / kSolveThreads), kSolveThreads, p->solve_smem, s>>>(
+            (const real*)p->X, p->knots, p->cnt, (const Fac<real>*)p->fac, (const real*)p->yb, (SY<real>*)p->sy, g,
+            k0, kc, p->S, p->H, p->GS, p->ngroups);
+        lc.end(MEMD_STAGE_SOLVE);
+        lc.begin();
+        launch_eval<real>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
+        lc.end(MEMD_STAGE_EVAL);
+    }
+}
+
+template <typename real>
+static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
+{
+    const Geom& g = p->g;
+    const size_t CL = (size_t)g.C * g.L;
+    const int nimf = (int)p->cfg.num_imfs;
+    const int maxit = (int)p->cfg.max_iter;
+    dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
+    for (int i = 0; i + 1 < nimf; ++i) {
+        cudaMemcpyAsync(p->X, p->run, CL * sizeof(real), cudaMemcpyDeviceToDevice, s);
+        for (int j = 0; j < maxit; ++j) {
+            memd_trace_entry* tr = p->trace_dev ? p->trace_dev + ((size_t)i * (maxit + 1) + j) * (size_t)g.K * 2 : nullptr;
+            enqueue_sift<real>(p, s, tr, lc);
+        }
+        lc.begin();
+        k_to_channel_major<real, real><<<tg, tb, 0, s>>>((const real*)p->X, (real*)p->imf + (size_t)i * CL,
+                                                         (real*)p->run, g.C, g.L);
+        lc.end(MEMD_STAGE_OTHER);
+    }
+    lc.begin();
+    k_to_channel_major<real, real><<<tg, tb, 0, s>>>((const real*)p->run, (real*)p->imf + (size_t)(nimf - 1) * CL,
+                                                     nullptr, g.C, g.L);
+    lc.end(MEMD_STAGE_OTHER);
+}
+
+template <typename real>
+static memd_status build_graph(memd_plan* p)
+{
+    if (p->exec) return MEMD_OK;
+    cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return set_cuda_error("graph: begin capture", e);
+    Launches lc;
+    enqueue_decomposition<real>(p, p->cap, lc);
+    p->graph_launches = lc.count;
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(p->cap, &graph);
+    if (e != cudaSuccess) return set_cuda_error("graph: end capture", e);
+    e = cudaGraphInstantiate(&p->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        p->exec = nullptr;
+        return set_cuda_error("graph: instantiate", e);
+    }
+    return MEMD_OK;
+}
+
+template <typename real, typename tin>
+static memd_status run_impl(memd_plan* p, const int32_t* d_x, const tin* d_y, const tin* d_dir, tin* d_imfs,
+                            void* stream, memd_stats* stats)
+{
+    if (!p) return set_error(MEMD_ERR_INVALID, "run: null plan");
+    if (!d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run: null pointer");
+    if ((int)sizeof(real) != p->real_bytes) return set_error(MEMD_ERR_PRECISION, "run: plan precision differs");
+    cudaStream_t s = (cudaStream_t)stream;
+    const Geom& g = p->g;
+    const size_t CL = (size_t)g.C * g.L;
+    cudaError_t e;
+    if (d_x) {
+        cudaMemsetAsync(p->coord_bad, 0, sizeof(int), s);
+        k_check_coords<<<64, 256, 0, s>>>(d_x, g.L, p->coord_bad);
+        cudaMemcpyAsync(p->host_flag, p->coord_bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return set_cuda_error("run: coordinate check", e);
+        if (*p->host_flag) return set_error(MEMD_ERR_COORD, "run: d_x must hold 0..L-1");
+    }
+    memd_status st = build_graph<real>(p);
+    if (st != MEMD_OK) return st;
+    cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
+    dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
+    k_to_sample_major<real, tin><<<tg, tb, 0, s>>>(d_y, (real*)p->run, g.C, g.L);
+    cudaMemcpyAsync(p->dir, d_dir, sizeof(real) * (size_t)g.K * g.C, cudaMemcpyDeviceToDevice, s);
+    cudaEventRecord(p->e0, s);
+    e = cudaGraphLaunch(p->exec, s);
+    if (e != cudaSuccess) return set_cuda_error("run: graph launch", e);
+    cudaEventRecord(p->e1, s);
+    cudaMemcpyAsync(d_imfs, p->imf, sizeof(real) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
+    if (p->trace_dev && p->trace_host)
+        cudaMemcpyAsync(p->trace_host, p->trace_dev, sizeof(memd_trace_entry) * p->trace_n, cudaMemcpyDeviceToHost, s);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error("run: launch", e);
+    if (stats || (p->trace_dev && p->trace_host)) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return set_cuda_error("run: synchronize", e);
+    }
+    if (stats) {
+        RunState hs;
+        e = cudaMemcpy(&hs, p->st, sizeof(RunState), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return set_cuda_error("run: read state", e);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->e0, p->e1);
+        memset(stats, 0, sizeof(*stats));
+        stats->elapsed_ms = ms;
+        stats->flags = hs.flags;
+        stats->n_imfs = (int)p->cfg.num_imfs - 1;
+        stats->launches = p->graph_launches + 1 + (d_x ? 1 : 0);
+        for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
+    }
+    return MEMD_OK;
+}
+
+template <typename real>
+static memd_status profile_impl(memd_plan* p, const real* d_y, const real* d_dir, real* d_imfs, void* stream,
+                                memd_profile* prof)
+{
+    if (!p || !d_y || !d_dir || !d_imfs || !prof) return set_error(MEMD_ERR_INVALID, "profile: null argument");
+    if ((int)sizeof(real) != p->real_bytes) return set_error(MEMD_ERR_PRECISION, "profile: plan precision differs");
+    cudaStream_t s = (cudaStream_t)stream;
+    const Geom& g = p->g;
+    const size_t CL = (size_t)g.C * g.L;
+    memset(prof, 0, sizeof(*prof));
+    Launches lc;
+    lc.prof = prof;
+    lc.s = s;
+    cudaEventCreate(&lc.a);
+    cudaEventCreate(&lc.b);
+    cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
+    dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
+    lc.begin();
+    k_to_sample_major<real, real><<<tg, tb, 0, s>>>(d_y, (real*)p->run, g.C, g.L);
+    lc.end(MEMD_STAGE_OTHER);
+    cudaMemcpyAsync(p->dir, d_dir, sizeof(real) * (size_t)g.K * g.C, cudaMemcpyDeviceToDevice, s);
+    memd_trace_entry* keep = p->trace_dev;
+    p->trace_dev = nullptr;
+    enqueue_decomposition<real>(p, s, lc);
+    p->trace_dev = keep;
+    cudaMemcpyAsync(d_imfs, p->imf, sizeof(real) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaEventDestroy(lc.a);
+    cudaEventDestroy(lc.b);
+    if (e != cudaSuccess) return set_cuda_error("profile: run", e);
+    return MEMD_OK;
+}
+
+}  // namespace memd
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+void memd_default_config(memd_config* cfg)
+{
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->num_imfs = 9;
+    cfg->max_iter = 10;
+    cfg->precision = MEMD_PREC_F64;
+    cfg->stop_mode = MEMD_STOP_FIXED;
+    cfg->stop_sd = 0.075;
+    cfg->stop_sd2 = 0.75;
+    cfg->stop_tol = 0.075;
+    cfg->ref_window = 1;
+}
+
+const char* memd_last_error(void) { return memd::g_err.c_str(); }
+
+const char* memd_version(void) { return "memd-gb300 0.1 (sm_103a)"; }
+
+memd_status memd_plan_destroy(memd_plan* p)
+{
+    if (!p) return MEMD_OK;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    for (void* a : p->allocs) cudaFree(a);
+    if (p->host_flag) cudaFreeHost(p->host_flag);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    if (p->e0) cudaEventDestroy(p->e0);
+    if (p->e1) cudaEventDestroy(p->e1);
+    delete p;
+    return MEMD_OK;
+}
+
+size_t memd_plan_workspace_bytes(const memd_plan* p) { return p ? p->bytes : 0; }
+
+memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
+{
+    using namespace memd;
+    if (!cfg || !out) return set_error(MEMD_ERR_INVALID, "plan: null argument");
+    *out = nullptr;
+    const memd_config c = *cfg;
+    if (c.channels < 1 || c.channels > 256) return set_error(MEMD_ERR_INVALID, "plan: channels must be in [1, 256]");
+    if (c.length < 4 || c.length > (1LL << 28)) return set_error(MEMD_ERR_INVALID, "plan: length must be in [4, 2^28]");
+    if (c.directions < 1 || c.directions > 65536) return set_error(MEMD_ERR_INVALID, "plan: directions must be in [1, 65536]");
+    if (c.num_imfs < 1 || c.num_imfs > 4096) return set_error(MEMD_ERR_INVALID, "plan: num_imfs must be in [1, 4096]");
+    if (c.max_iter < 0 || c.max_iter > 100000) return set_error(MEMD_ERR_INVALID, "plan: max_iter must be in [0, 100000]");
+    if (c.precision < MEMD_PREC_F64 || c.precision > MEMD_PREC_MIXED) return set_error(MEMD_ERR_INVALID, "plan: bad precision");
+    if (c.stop_mode != MEMD_STOP_FIXED) return set_error(MEMD_ERR_UNSUPPORTED, "plan: stop criterion not built in this library");
+    memd_plan* p = new memd_plan();  // value-initialised: every pointer and count starts at zero
+    p->cfg = c;
+    const int C = (int)c.channels, L = (int)c.length, K = (int)c.directions;
+    p->real_bytes = (c.precision == MEMD_PREC_F64) ? 8 : 4;
+    p->g.C = C;
+    p->g.L = L;
+    p->g.K = K;
+    p->g.W = (L + 31) / 32;
+    p->g.cap = (L + 1) / 2 + 4;
+    p->g.cov = c.ref_window ? 240 * ((L + 241) / 242) : L;
+    p->Kc = (c.dir_chunk > 0) ? std::min<int>((int)c.dir_chunk, K) : K;
+    p->Kc = std::min(p->Kc, 1024);
+    p->nchunks = (K + p->Kc - 1) / p->Kc;
+    const bool f64 = p->real_bytes == 8;
+    if (c.solve_window < 0) {
+        p->S = p->g.cap;
+        p->H = -1;
+        p->Sf = p->g.cap;
+        p->Hf = -1;
+    } else {
+        p->S = 256;
+        p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : 24);
+        p->Sf = 256;
+        p->Hf = f64 ? 40 : 20;
+    }
+    p->GS = std::min(32, next_pow2(C));
+    p->ngroups = (C + p->GS - 1) / p->GS;
+    // eval tile: G channels x T samples, enough CTAs to fill the GPU
+    p->evalG = std::min(32, std::max(4, next_pow2(C)));
+    {
+        const int NR = 256 / p->evalG;
+        const int groups = (C + p->evalG - 1) / p->evalG;
+        int best = -1, bestT = 0;
+        const int spts[3] = {2, 4, 8};
+        for (int i = 0; i < 3; ++i) {
+            const int T = NR * spts[i];
+            if (T % 32 != 0 || T > 512) continue;
+            const long ctas = (long)((L + T - 1) / T) * groups;
+            if (best < 0) { best = spts[i]; bestT = T; }
+            if (ctas >= 608) { best = spts[i]; bestT = T; }
+        }
+        p->evalSPT = best;
+        p->evalT = bestT;
+    }
+    const size_t rb = (size_t)p->real_bytes;
+    p->proj_smem = rb * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2));
+    p->solve_smem = p->H > 0 ? rb * (size_t)p->H * kSolveThreads : 0;
+    const size_t CL = (size_t)C * L;
+    const size_t Kc = (size_t)p->Kc;
+    memd_status st = MEMD_OK;
+#define ALLOC(ptr, bytes)                                        \
+    do {                                                         \
+        if (st == MEMD_OK) st = dev_alloc(p, (void**)&(ptr), (bytes)); \
+    } while (0)
+    ALLOC(p->X, rb * CL);
+    ALLOC(p->run, rb * CL);
+    ALLOC(p->dir, rb * (size_t)K * C);
+    if (p->nchunks > 1) ALLOC(p->acc, rb * CL);
+    ALLOC(p->imf, rb * CL * (size_t)c.num_imfs);
+    ALLOC(p->bits, sizeof(uint32_t) * 2 * Kc * p->g.W);
+    ALLOC(p->wpref, sizeof(int) * 2 * Kc * (p->g.W + 1));
+    ALLOC(p->knots, sizeof(int) * 2 * Kc * p->g.cap);
+    ALLOC(p->cnt, sizeof(int) * 2 * (size_t)K);
+    ALLOC(p->yb, rb * 2 * Kc * 2 * C);
+    ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
+    ALLOC(p->sy, rb * 2 * 2 * Kc * p->g.cap * C);
+    ALLOC(p->rtab, rb * (size_t)(L + 1));
+    ALLOC(p->st, sizeof(RunState));
+    ALLOC(p->coord_bad, sizeof(int));
+#undef ALLOC
+    if (st != MEMD_OK) {
+        memd_plan_destroy(p);
+        return st;
+    }
+    cudaError_t e = cudaMallocHost((void**)&p->host_flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&p->e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&p->e1);
+    if (e == cudaSuccess) e = f64 ? set_attrs<double>(p) : set_attrs<float>(p);
+    if (e == cudaSuccess) {
+        // reciprocal table 1/h, h = 0..L (h = 0 unused)
+        double* r64 = nullptr;
+        float* r32 = nullptr;
+        e = cudaMalloc((void**)&r64, sizeof(double) * (size_t)(L + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&r32, sizeof(float) * (size_t)(L + 1));
+        if (e == cudaSuccess) {
+            k_fill_reciprocals<<<256, 256>>>(r64, r32, L + 1);
+            e = cudaMemcpy(p->rtab, f64 ? (void*)r64 : (void*)r32, rb * (size_t)(L + 1), cudaMemcpyDeviceToDevice);
+        }
+        cudaFree(r64);
+        cudaFree(r32);
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        memd_plan_destroy(p);
+        return set_cuda_error("plan: setup", e);
+    }
+    *out = p;
+    return MEMD_OK;
+}
+
+memd_status memd_plan_set_trace(memd_plan* p, memd_trace_entry* host_trace)
+{
+    using namespace memd;
+    if (!p) return set_error(MEMD_ERR_INVALID, "trace: null plan");
+    if (p->exec) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+    }
+    p->trace_host = host_trace;
+    if (!host_trace) {
+        p->trace_dev = nullptr;
+        return MEMD_OK;
+    }
+    p->trace_n = (size_t)p->cfg.num_imfs * (size_t)(p->cfg.max_iter + 1) * (size_t)p->g.K * 2;
+    if (!p->trace_dev) {
+        memd_status st = dev_alloc(p, (void**)&p->trace_dev, sizeof(memd_trace_entry) * p->trace_n);
+        if (st != MEMD_OK) return st;
+    }
+    cudaMemset(p->trace_dev, 0, sizeof(memd_trace_entry) * p->trace_n);
+    return MEMD_OK;
+}
+
+memd_status memd_run_f64(memd_plan* plan, const int32_t* d_x, const double* d_y, const double* d_dir,
+                         double* d_imfs, void* stream, memd_stats* stats)
+{
+    return memd::run_impl<double, double>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
+}
+
+memd_status memd_run_f32(memd_plan* plan, const int32_t* d_x, const float* d_y, const float* d_dir,
+                         float* d_imfs, void* stream, memd_stats* stats)
+{
+    return memd::run_impl<float, float>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
+}
+
+memd_status memd_profile_f64(memd_plan* plan, const double* d_y, const double* d_dir, double* d_imfs,
+                             void* stream, memd_profile* prof)
+{
+    return memd::profile_impl<double>(plan, d_y, d_dir, d_imfs, stream, prof);
+}
+
+memd_status memd_profile_f32(memd_plan* plan, const float* d_y, const float* d_dir, float* d_imfs,
+                             void* stream, memd_profile* prof)
+{
+    return memd::profile_impl<float>(plan, d_y, d_dir, d_imfs, stream, prof);
+}
+
+memd_status memd_run_batched_f64(memd_plan*, int32_t, const int64_t*, const int64_t*, const double*,
+                                 const double*, double*, void*, memd_stats*)
+{
+    return memd::set_error(MEMD_ERR_UNSUPPORTED, "batched runs are not built in this library");
+}
+
+memd_status memd_run_batched_f32(memd_plan*, int32_t, const int64_t*, const int64_t*, const float*,
+                                 const float*, float*, void*, memd_stats*)
+{
+    return memd::set_error(MEMD_ERR_UNSUPPORTED, "batched runs are not built in this library");
+}
+
+}  // extern "C"

@@ -1,0 +1,603 @@
+// memd_kernels.cuh -- the per-sift kernels of the GB300 MEMD engine.
+//
+// One sift (reference loop body memReducedEpochs_dev.cu:1179-1327) is five
+// launches per direction chunk, all templated on the arithmetic type:
+//
+//   k_project_extrema  projection P = dir . X for a tile of samples and
+//                      directions, strict-extremum tests, warp ballots into
+//                      one 32-bit word per (direction, 32 samples)
+//                      (REF:1182-1184 + REF:77-141)
+//   k_compact          per (direction, envelope): popcount prefix of the
+//                      bitmask, ordered knot list, knot count, end-point clamp
+//                      of the knot values, optional trace (REF:143-486, 545-584)
+//   k_factor           channel-independent Thomas factorisation of the
+//                      natural-spline system (REF:704-736; replaces the
+//                      factorisation inside cusparse gtsv2_nopivot)
+//   k_solve            forward/backward substitution for every channel, in
+//                      windows of S knots with an H-knot halo (REF:1227-1241)
+//   k_eval             spline coefficients per interval, envelope evaluation
+//                      fused with the mean over directions and the update of
+//                      the working signal (REF:775-864)
+//
+// Working layout in HBM (sample-major, channel-minor, so that a knot's C
+// values are one contiguous row):
+//   X[n][c]                         working signal (n < L, c < C)
+//   bits[env][kk][w]                extrema bitmask, bit j of word w = sample 32w+j
+//   wpref[env][kk][w]               knots before word w (w <= W)
+//   knots[env][kk][i]               knot sample indices, i < E <= cap
+//   fac[env][kk][i]                 Fac<real> per knot row
+//   sy[env][kk][i][c]               SY<real> per knot and channel
+//   yb[env][kk][2][c]               clamped end-knot values
+// env 0 = maxima (upper envelope), 1 = minima (lower envelope); kk indexes the
+// directions of the current chunk, counts cnt[env][k] use the global k.
+#pragma once
+
+#include "memd_device.cuh"
+
+namespace memd {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kTrace = 1;
+
+// ---------------------------------------------------------------------------
+// Projection + extrema bitmasks.  CTA tile: 64 samples x 16 directions,
+// 8 warps = 2 sample groups x 4 direction groups of 4 directions; warp 0 also
+// computes the two halo samples (n0-1, n0+64) for all 16 directions.
+// P is summed over channels in index order with fma, like the oracle.
+// ---------------------------------------------------------------------------
+constexpr int kProjTN = 64;
+constexpr int kProjTK = 16;
+
+template <typename real>
+__global__ void __launch_bounds__(256)
+k_project_extrema(const real* __restrict__ X, const real* __restrict__ dir,
+                  uint32_t* __restrict__ bits, Geom g, int k0, int Kc)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int C = g.C;
+    const int ldx = C + 1;  // odd stride: lanes reading different rows hit different banks
+    real* xs = reinterpret_cast<real*>(smem_raw);          // (TN + 2) x ldx
+    real* ds = xs + (kProjTN + 2) * ldx;                     // TK x C
+    real* ps = ds + kProjTK * C;                              // TK x (TN + 2)
+    const int n0 = blockIdx.x * kProjTN;
+    const int kt0 = blockIdx.y * kProjTK;
+    for (int idx = threadIdx.x; idx < (kProjTN + 2) * C; idx += blockDim.x) {
+        const int r = idx / C, c = idx - r * C;
+        const int n = n0 - 1 + r;
+        xs[r * ldx + c] = (n >= 0 && n < g.L) ? X[(size_t)n * C + c] : real(0);
+    }
+    for (int idx = threadIdx.x; idx < kProjTK * C; idx += blockDim.x) {
+        const int kk = idx / C, c = idx - kk * C;
+        const int k = kt0 + kk;
+        ds[idx] = (k < Kc) ? dir[(size_t)(k0 + k) * C + c] : real(0);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sg = warp & 1, dg = warp >> 1;
+    {
+        const int r = 1 + sg * 32 + lane;
+        real acc[4] = {real(0), real(0), real(0), real(0)};
+        const real* xr = xs + r * ldx;
+        const real* d0 = ds + (dg * 4) * C;
+        for (int c = 0; c < C; ++c) {
+            const real xv = xr[c];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[j] = fmad_(xv, d0[j * C + c], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ps[(dg * 4 + j) * (kProjTN + 2) + r] = acc[j];
+    }
+    if (warp == 0) {
+        const int side = lane >> 4, kk = lane & 15;
+        const int r = side ? kProjTN + 1 : 0;
+        real acc = real(0);
+        const real* xr = xs + r * ldx;
+        const real* dd = ds + kk * C;
+        for (int c = 0; c < C; ++c) acc = fmad_(xr[c], dd[c], acc);
+        ps[kk * (kProjTN + 2) + r] = acc;
+    }
+    __syncthreads();
+    const int n = n0 + sg * 32 + lane;
+    const int r = 1 + sg * 32 + lane;
+    const int last = min(g.cov, g.L - 2);
+    const bool inrange = n < g.L;
+    const bool endpt = (n == 0) || (n == g.L - 1);
+    const bool interior = (n >= 1) && (n <= last);
+    const int w = (n0 >> 5) + sg;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int kk = dg * 4 + j;
+        const real* pr = ps + kk * (kProjTN + 2);
+        const real p = pr[r], pl = pr[r - 1], pn = pr[r + 1];
+        const bool mx = inrange && (endpt || (interior && p > pl && p > pn));
+        const bool mn = inrange && (endpt || (interior && p < pl && p < pn));
+        const uint32_t wmax = __ballot_sync(kFull, mx);
+        const uint32_t wmin = __ballot_sync(kFull, mn);
+        if (lane == 0 && kt0 + kk < Kc && w < g.W) {
+            bits[(size_t)(kt0 + kk) * g.W + w] = wmax;
+            bits[(size_t)(Kc + kt0 + kk) * g.W + w] = wmin;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Knot lists.  One CTA of 512 threads per (envelope, direction).
+// ---------------------------------------------------------------------------
+template <typename real>
+__global__ void __launch_bounds__(512)
+k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __restrict__ knots,
+          int* __restrict__ cnt, real* __restrict__ yb, const real* __restrict__ X,
+          memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st)
+{
+    const int env = blockIdx.x / Kc, kk = blockIdx.x - env * Kc;
+    const size_t slot = (size_t)env * Kc + kk;
+    const uint32_t* b = bits + slot * g.W;
+    int* wp = wpref + slot * (g.W + 1);
+    int* kn = knots + slot * g.cap;
+    const int per = (g.W + blockDim.x - 1) / blockDim.x;
+    const int wb = threadIdx.x * per, we = min(g.W, wb + per);
+    int local = 0;
+    for (int w = wb; w < we; ++w) local += __popc(b[w]);
+    __shared__ int wsum[16];
+    __shared__ unsigned long long hsum[16];
+    __shared__ int total_s;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        const int v = lane < nw ? wsum[lane] : 0;
+        int iv = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, iv, o);
+            if (lane >= o) iv += t;
+        }
+        if (lane < nw) wsum[lane] = iv - v;
+        if (lane == nw - 1) total_s = iv;
+    }
+    __syncthreads();
+    int run = wsum[wid] + incl - local;
+    uint64_t h = 0;
+    for (int w = wb; w < we; ++w) {
+        wp[w] = run;
+        uint32_t word = b[w];
+        while (word) {
+            const int j = __ffs(word) - 1;
+            word &= word - 1u;
+            const int n = w * 32 + j;
+            if (run < g.cap) kn[run] = n;
+            ++run;
+            h += splitmix64((uint64_t)(uint32_t)n);
+        }
+    }
+    const int E = total_s;
+    h = warp_sum<unsigned long long>(h);
+    if (lane == 0) hsum[wid] = h;
+    if (threadIdx.x == 0) {
+        wp[g.W] = E;
+        cnt[env * g.K + k0 + kk] = E;
+        if (E > g.cap) atomicOr(&st->flags, 2);
+    }
+    __syncthreads();
+    if (trace && threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += hsum[i];
+        memd_trace_entry e;
+        e.count = E;
+        e.flags = 0;
+        e.hash = t;
+        trace[(size_t)(k0 + kk) * 2 + env] = e;
+    }
+    if (E > g.cap || E < 2) return;
+    // End-point clamp of the knot values (REF:447-486 max, 545-584 min).
+    for (int c = threadIdx.x; c < g.C; c += blockDim.x) {
+        real v0 = X[(size_t)kn[0] * g.C + c];
+        real vE = X[(size_t)kn[E - 1] * g.C + c];
+        if (E - 1 > 4) {
+            const real v1 = X[(size_t)kn[1] * g.C + c];
+            const real v2 = X[(size_t)kn[2] * g.C + c];
+            real slope = div_(sub_(v2, v1), real(kn[2] - kn[1]));
+            real t = fmad_(-slope, real(kn[1] - kn[0]), v1);
+            if (env == 0 ? (t > v0) : (t < v0)) v0 = t;
+            const real a = X[(size_t)kn[E - 3] * g.C + c];
+            const real bb = X[(size_t)kn[E - 2] * g.C + c];
+            slope = div_(sub_(bb, a), real(kn[E - 2] - kn[E - 3]));
+            t = fmad_(slope, real(kn[E - 1] - kn[E - 2]), bb);
+            if (env == 0 ? (t > vE) : (t < vE)) vE = t;
+        }
+        yb[(slot * 2 + 0) * g.C + c] = v0;
+        yb[(slot * 2 + 1) * g.C + c] = vE;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Channel-independent factorisation.  One thread per (envelope, direction,
+// segment of Sf rows); the pivot recurrence starts Hf rows early (exact when
+// the window reaches row 0, whose pivot is 1 with cp = 0; otherwise the
+// start error decays by at least 1/3 per row).  rtab[h] = 1/h.
+// ---------------------------------------------------------------------------
+template <typename real>
+__global__ void __launch_bounds__(128)
+k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real* __restrict__ rtab,
+         Fac<real>* __restrict__ fac, Geom g, int k0, int Kc, int Sf, int Hf)
+{
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nseg = (g.cap + Sf - 1) / Sf;
+    const int seg = (int)(gid % nseg);
+    const long rest = gid / nseg;
+    const int kk = (int)(rest % Kc);
+    const int env = (int)(rest / Kc);
+    if (env >= 2) return;
+    const int E = cnt[env * g.K + k0 + kk];
+    if (E > g.cap) return;
+    const int i0 = seg * Sf;
+    if (i0 >= E) return;
+    const int i1 = min(E, i0 + Sf);
+    const size_t slot = (size_t)env * Kc + kk;
+    const int* x = knots + slot * g.cap;
+    Fac<real>* f = fac + slot * g.cap;
+    const int js = (Hf < 0) ? 0 : max(0, i0 - Hf);
+    real cp = real(0);
+    int xl = js > 0 ? x[js - 1] : 0;
+    int xi = x[js];
+    for (int i = js; i < i1; ++i) {
+        const int xr = (i < E - 1) ? x[i + 1] : xi;
+        real l, d, u;
+        if (i == 0 || i == E - 1) {
+            l = real(0); d = real(1); u = real(0);
+        } else {
+            const int hl = xi - xl, hr = xr - xi;
+            l = real(hl); u = real(hr); d = real(2 * (hl + hr));
+        }
+        const real gp = fmad_(-l, cp, d);
+        const real m = div_(real(1), gp);
+        cp = mul_(u, m);
+        if (i >= i0) {
+            Fac<real> o;
+            o.m = m;
+            o.lm = mul_(l, m);
+            o.cp = cp;
+            o.ih = (i < E - 1) ? rtab[xr - xi] : real(0);
+            f[i] = o;
+        }
+        xl = xi;
+        xi = xr;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Substitution.  A group of GS lanes (GS | 32) handles one (envelope,
+// direction, segment, channel group); each lane one channel.  The forward
+// sweep runs over [i0-H, i1+H), the backward sweep from i1+H-1 down to i0;
+// both recurrences contract (multipliers <= 2/3 and <= 1/2 per row), so the
+// window's truncated starts perturb the segment by at most that factor to the
+// power H.  H < 0 selects the exact single-window solve.
+// The halo values of the forward sweep live in shared memory, the segment's
+// own values go straight to sy and are overwritten by the solution.
+// ---------------------------------------------------------------------------
+constexpr int kSolveThreads = 128;
+
+template <typename real>
+__global__ void __launch_bounds__(kSolveThreads)
+k_solve(const real* __restrict__ X, const int* __restrict__ knots, const int* __restrict__ cnt,
+        const Fac<real>* __restrict__ fac, const real* __restrict__ yb, SY<real>* __restrict__ sy,
+        Geom g, int k0, int Kc, int S, int H, int GS, int ngroups)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    real* halo = reinterpret_cast<real*>(smem_raw);  // [max(H,0)][kSolveThreads]
+    const long gl = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = (int)(gl % GS);
+    long item = gl / GS;
+    const int nseg = (g.cap + S - 1) / S;
+    const int cgi = (int)(item % ngroups);
+    item /= ngroups;
+    const int seg = (int)(item % nseg);
+    item /= nseg;
+    const int kk = (int)(item % Kc);
+    const int env = (int)(item / Kc);
+    if (env >= 2) return;
+    const int E = cnt[env * g.K + k0 + kk];
+    if (E > g.cap || E < 2) return;
+    const int i0 = seg * S;
+    if (i0 >= E) return;
+    const int i1 = min(E, i0 + S);
+    const int c = cgi * GS + lane;
+    if (c >= g.C) return;
+    const int C = g.C;
+    const size_t slot = (size_t)env * Kc + kk;
+    const int* x = knots + slot * g.cap;
+    const Fac<real>* f = fac + slot * g.cap;
+    SY<real>* o = sy + slot * (size_t)g.cap * C;
+    const real y0b = yb[(slot * 2 + 0) * C + c];
+    const real yEb = yb[(slot * 2 + 1) * C + c];
+    const int is = (H < 0) ? 0 : max(0, i0 - H);
+    const int ie = (H < 0) ? E : min(E, i1 + H);
+    auto Y = [&](int i) -> real {
+        return i == 0 ? y0b : (i == E - 1 ? yEb : X[(size_t)x[i] * C + c]);
+    };
+    real yi = Y(is);
+    real slope_prev = real(0);
+    if (is > 0) slope_prev = mul_(sub_(yi, Y(is - 1)), f[is - 1].ih);
+    real dprev = real(0);
+    real ynext = (is < E - 1) ? Y(is + 1) : real(0);
+    for (int i = is; i < ie; ++i) {
+        const Fac<real> fi = f[i];
+        // prefetch the knot value after next while this row is processed
+        const real yafter = (i + 2 < E) ? Y(i + 2) : real(0);
+        real slope = real(0), r = real(0);
+        if (i < E - 1) slope = mul_(sub_(ynext, yi), fi.ih);
+        if (i > 0 && i < E - 1) r = mul_(real(3), sub_(slope, slope_prev));
+        const real dcur = fmad_(-fi.lm, dprev, mul_(fi.m, r));
+        if (i < i1) {
+            SY<real> v;
+            v.s = dcur;
+            v.y = yi;
+            o[(size_t)i * C + c] = v;
+        } else {
+            halo[(i - i1) * kSolveThreads + threadIdx.x] = dcur;
+        }
+        slope_prev = slope;
+        yi = ynext;
+        ynext = yafter;
+        dprev = dcur;
+    }
+    real snext = real(0);
+    for (int i = ie - 1; i >= i0; --i) {
+        const real d = (i >= i1) ? halo[(i - i1) * kSolveThreads + threadIdx.x] : o[(size_t)i * C + c].s;
+        const real s = fmad_(-f[i].cp, snext, d);
+        if (i < i1) o[(size_t)i * C + c].s = s;
+        snext = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Envelope evaluation fused with the mean over directions and the update.
+// CTA: T = (256/G)*SPT samples x G channels; thread (row, ch) owns SPT
+// consecutive samples of one channel and keeps their running sum over the
+// directions in registers.  Per (direction, envelope):
+//   (a) the tile's knots, 1/h and bit words into shared memory,
+//   (b) interval index and offset t per sample; coefficients
+//       a = y_i, b = (y_{i+1}-y_i)/h - h(2 s_i + s_{i+1})/3, c = s_i,
+//       d = (s_{i+1} - s_i)/(3h) per (interval, channel),
+//   (c) S = fma(fma(fma(d, t, c), t, b), t, a) per (sample, channel).
+// The sum over qualified directions (E_max > 3 && E_min > 3) runs in
+// direction order; the last chunk applies X -= (sum/2)/Q (REF:832-864).
+// ---------------------------------------------------------------------------
+template <typename real, int G, int SPT>
+struct EvalShape {
+    static constexpr int NR = 256 / G;
+    static constexpr int T = NR * SPT;
+    static constexpr int MI = T / 2 + 4;
+    static size_t smem_bytes(int Kc)
+    {
+        return sizeof(real) * ((size_t)MI * 4 * G + T + MI) + sizeof(int) * ((size_t)(MI + 1) + T + T / 32 + 6 * Kc + 4);
+    }
+};
+
+template <typename real, int G, int SPT>
+__global__ void __launch_bounds__(256)
+k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restrict__ bits,
+       const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
+       const Fac<real>* __restrict__ fac, const SY<real>* __restrict__ sy, Geom g, int k0, int Kc,
+       int first_chunk, int last_chunk, RunState* st)
+{
+    using Sh = EvalShape<real, G, SPT>;
+    constexpr int T = Sh::T;
+    constexpr int MI = Sh::MI;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    real* coef = reinterpret_cast<real*>(smem_raw);  // [MI][4][G]
+    real* tts = coef + MI * 4 * G;                    // [T]
+    real* ihs = tts + T;                              // [MI]
+    int* kx = reinterpret_cast<int*>(ihs + MI);       // [MI + 1]
+    int* lis = kx + MI + 1;                           // [T]
+    uint32_t* wds = reinterpret_cast<uint32_t*>(lis + T);  // [T/32]
+    int* tab = reinterpret_cast<int*>(wds + T / 32);  // [2*Kc][3]
+    int* sQ = tab + 6 * Kc;
+
+    const int n0 = blockIdx.x * T;
+    const int cg = blockIdx.y;
+    const int cc = threadIdx.x % G;
+    const int row = threadIdx.x / G;
+    const int c = cg * G + cc;
+    const bool cok = c < g.C;
+    const int nl = min(T, g.L - n0);
+    const int C = g.C;
+    const real third = real(1.0 / 3.0);
+
+    for (int idx = threadIdx.x; idx < 2 * Kc; idx += blockDim.x) {
+        const int env = idx / Kc, kk = idx - env * Kc;
+        const size_t slot = (size_t)env * Kc + kk;
+        const int* wp = wpref + slot * (g.W + 1);
+        const uint32_t* b = bits + slot * g.W;
+        const int cl0 = wp[n0 >> 5];
+        const int nlast = n0 + nl - 1;
+        const int wl = nlast >> 5, jl = nlast & 31;
+        const int cll = wp[wl] + __popc(b[wl] & ((1u << jl) - 1u));
+        tab[idx * 3 + 0] = max(cl0 - 1, 0);
+        tab[idx * 3 + 1] = max(cll - 1, 0);
+        tab[idx * 3 + 2] = cl0;
+    }
+    if (threadIdx.x < 32) {
+        int q = 0;
+        for (int k = threadIdx.x; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        q = warp_sum(q);
+        if (threadIdx.x == 0) sQ[0] = q;
+    }
+    real acc[SPT];
+    real u[SPT];
+#pragma unroll
+    for (int j = 0; j < SPT; ++j) {
+        const int t = row * SPT + j;
+        acc[j] = real(0);
+        u[j] = real(0);
+        if (!first_chunk && cok && t < nl) acc[j] = acc_buf[(size_t)(n0 + t) * C + c];
+    }
+    __syncthreads();
+
+    for (int kk = 0; kk < Kc; ++kk) {
+        const int k = k0 + kk;
+        const int Emax = cnt[k], Emin = cnt[g.K + k];
+        if (!(Emax > 3 && Emin > 3)) continue;
+        if (Emax > g.cap || Emin > g.cap) continue;
+#pragma unroll
+        for (int env = 0; env < 2; ++env) {
+            const size_t slot = (size_t)env * Kc + kk;
+            const int ia = tab[(env * Kc + kk) * 3 + 0];
+            const int ib = tab[(env * Kc + kk) * 3 + 1];
+            const int cl0 = tab[(env * Kc + kk) * 3 + 2];
+            int m = ib - ia + 1;
+            if (m > MI - 1) {
+                if (threadIdx.x == 0) atomicOr(&st->flags, 2);
+                m = MI - 1;
+            }
+            const int* kn = knots + slot * g.cap;
+            const Fac<real>* fc = fac + slot * g.cap;
+            const SY<real>* sv = sy + slot * (size_t)g.cap * C;
+            const uint32_t* b = bits + slot * g.W;
+            __syncthreads();
+            for (int j = threadIdx.x; j <= m; j += blockDim.x) kx[j] = kn[ia + j];
+            for (int j = threadIdx.x; j < m; j += blockDim.x) ihs[j] = fc[ia + j].ih;
+            if (threadIdx.x < T / 32) {
+                const int w = (n0 >> 5) + threadIdx.x;
+                wds[threadIdx.x] = (w < g.W) ? b[w] : 0u;
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < nl; t += blockDim.x) {
+                const int w = t >> 5, jb = t & 31;
+                int cntl = 0;
+                for (int q = 0; q < w; ++q) cntl += __popc(wds[q]);
+                cntl += __popc(wds[w] & ((1u << jb) - 1u));
+                const int iv = max(cl0 + cntl - 1, 0);
+                int li = iv - ia;
+                li = min(li, m - 1);
+                lis[t] = li;
+                tts[t] = real(n0 + t - kx[li]);
+            }
+            for (int it = threadIdx.x; it < m * G; it += blockDim.x) {
+                const int li = it / G, ch = it - li * G;
+                const int cch = cg * G + ch;
+                if (cch < C) {
+                    const int i = ia + li;
+                    const SY<real> p0 = sv[(size_t)i * C + cch];
+                    const SY<real> p1 = sv[(size_t)(i + 1) * C + cch];
+                    const real h = real(kx[li + 1] - kx[li]);
+                    const real ih = ihs[li];
+                    const real slope = mul_(sub_(p1.y, p0.y), ih);
+                    const real bq = fmad_(-mul_(h, third), fmad_(real(2), p0.s, p1.s), slope);
+                    const real dq = mul_(sub_(p1.s, p0.s), mul_(ih, third));
+                    real* cf = coef + (size_t)li * 4 * G + ch;
+                    cf[0] = p0.y;
+                    cf[G] = bq;
+                    cf[2 * G] = p0.s;
+                    cf[3 * G] = dq;
+                }
+            }
+            __syncthreads();
+            if (cok) {
+#pragma unroll
+                for (int j = 0; j < SPT; ++j) {
+                    const int t = row * SPT + j;
+                    if (t < nl) {
+                        const int li = lis[t];
+                        const real tt = tts[t];
+                        const real* cf = coef + (size_t)li * 4 * G + cc;
+                        const real v = fmad_(fmad_(fmad_(cf[3 * G], tt, cf[2 * G]), tt, cf[G]), tt, cf[0]);
+                        if (env == 0) u[j] = v;
+                        else acc[j] = add_(acc[j], add_(u[j], v));
+                    }
+                }
+            }
+        }
+    }
+    const int Q = sQ[0];
+    if (last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
+    if (!cok) return;
+#pragma unroll
+    for (int j = 0; j < SPT; ++j) {
+        const int t = row * SPT + j;
+        if (t < nl) {
+            const size_t idx = (size_t)(n0 + t) * C + c;
+            if (last_chunk) {
+                const real val = mul_(acc[j], real(0.5));
+                X[idx] = sub_(X[idx], div_(val, real(Q)));
+            } else {
+                acc_buf[idx] = acc[j];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Layout transforms and IMF bookkeeping (REF:1174, 1178, 1328-1338).
+// 32 x 32 tiles through shared memory; block (32, 8).
+// ---------------------------------------------------------------------------
+// run[n][c] = (real) y[c][n]
+template <typename real, typename tin>
+__global__ void k_to_sample_major(const tin* __restrict__ y, real* __restrict__ run, int C, int L)
+{
+    __shared__ real tile[32][33];
+    const int n_base = blockIdx.x * 32, c_base = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int c = c_base + r, n = n_base + threadIdx.x;
+        if (c < C && n < L) tile[r][threadIdx.x] = real(y[(size_t)c * L + n]);
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int n = n_base + r, c = c_base + threadIdx.x;
+        if (c < C && n < L) run[(size_t)n * C + c] = tile[threadIdx.x][r];
+    }
+}
+
+// out[c][n] = src[n][c]; when upd != nullptr also upd[n][c] -= src[n][c]
+template <typename real, typename tout>
+__global__ void k_to_channel_major(const real* __restrict__ src, tout* __restrict__ out,
+                                   real* __restrict__ upd, int C, int L)
+{
+    __shared__ real tile[32][33];
+    const int n_base = blockIdx.x * 32, c_base = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int n = n_base + r, c = c_base + threadIdx.x;
+        if (c < C && n < L) {
+            const size_t idx = (size_t)n * C + c;
+            const real v = src[idx];
+            tile[r][threadIdx.x] = v;
+            if (upd) upd[idx] = sub_(upd[idx], v);
+        }
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int c = c_base + r, n = n_base + threadIdx.x;
+        if (c < C && n < L) out[(size_t)c * L + n] = tout(tile[threadIdx.x][r]);
+    }
+}
+
+__global__ void k_check_coords(const int32_t* __restrict__ x, int L, int* __restrict__ bad)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < L; n += gridDim.x * blockDim.x)
+        if (x[n] != n) atomicOr(bad, 1);
+}
+
+__global__ void k_fill_reciprocals(double* __restrict__ r64, float* __restrict__ r32, int n)
+{
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < n; h += gridDim.x * blockDim.x) {
+        r64[h] = h > 0 ? __ddiv_rn(1.0, (double)h) : 0.0;
+        r32[h] = h > 0 ? __fdiv_rn(1.0f, (float)h) : 0.0f;
+    }
+}
+
+__global__ void k_set_sifts(RunState* st, int imf, int sifts)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st->sifts[imf < 64 ? imf : 63] = sifts;
+        st->n_imfs = imf + 1;
+    }
+}
+
+}  // namespace memd

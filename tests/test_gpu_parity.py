@@ -1,0 +1,159 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference build's
+goldens and the CPU oracle.
+
+Bar for the FP64 path: identical extrema index sets at every sift (knot count
+and set hash per direction and envelope), IMFs within 1e-10 relative L2.
+"""
+import numpy as np
+import pytest
+
+import make_golden
+import memd_gb300 as mg
+import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+CASES = [c["name"] for c in make_golden.CASES]
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def run_gpu(y, dirs, nimf, max_iter, precision=mg.PREC_F64, trace=False, x=None, **kw):
+    C, L = y.shape
+    K = dirs.shape[0]
+    tdt = torch.float64 if precision == mg.PREC_F64 else torch.float32
+    plan = mg.Plan(C, L, K, nimf, max_iter, precision=precision, **kw)
+    if trace:
+        plan.set_trace(True)
+    dy = torch.as_tensor(np.ascontiguousarray(y), dtype=tdt).cuda()
+    dd = torch.as_tensor(np.ascontiguousarray(dirs), dtype=tdt).cuda()
+    out = torch.empty((nimf, C, L), dtype=tdt, device="cuda")
+    st = plan.run(dy, dd, out, x=x)
+    res = out.cpu().numpy()
+    tr = plan.trace().copy() if trace else None
+    plan.close()
+    return res, st, tr
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_f64_matches_reference_build(name):
+    g = make_golden.load_case(name)
+    imfs, st, tr = run_gpu(g["in_f64"], g["dirs_f64"], g["nimf"], g["max_iter"], trace=True)
+    for i in range(g["nimf"]):
+        assert rel_l2(imfs[i], g["ref_f64"][i]) < 1e-10, (name, i)
+    # extrema index sets, sift by sift, against the oracle on the same input
+    _, info = oracle.memd(g["in_f64"], g["dirs_f64"], g["nimf"], g["max_iter"], trace=True)
+    otr = info["trace"]
+    assert np.array_equal(tr["count"], otr["count"])
+    assert np.array_equal(tr["hash"], otr["hash"])
+    assert st.n_imfs == g["nimf"] - 1 and st.flags == 0
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_f32_close_to_reference_build(name):
+    g = make_golden.load_case(name)
+    imfs, st, _ = run_gpu(g["in_f32"], g["dirs_f32"], g["nimf"], g["max_iter"], precision=mg.PREC_F32)
+    for i in range(g["nimf"]):
+        assert rel_l2(imfs[i], g["ref_f32"][i]) < 5e-4, (name, i)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_directions_match_reference(name):
+    g = make_golden.load_case(name)
+    d64 = mg.directions(g["C"], g["K"], dtype="f64").cpu().numpy()
+    d32 = mg.directions(g["C"], g["K"], dtype="f32").cpu().numpy()
+    assert np.abs(d64 - g["dirs_f64"]).max() < 1e-14
+    assert np.abs(d32 - g["dirs_f32"]).max() < 2e-6
+
+
+def test_directions_mex_convention():
+    primes = [2, 3, 5, 7, 11, 13]
+    d = mg.directions(6, 40, primes=primes, dtype="f64").cpu().numpy()
+    o = oracle.directions(6, 40, primes=primes)
+    assert np.abs(d - o).max() < 1e-14
+
+
+def eeg(C, L, seed=0, fs=256.0):
+    return mg.synth_eeg(C, L, fs, seed)
+
+
+@pytest.mark.parametrize("C,L,K", [(5, 4097, 17), (32, 30504, 128), (3, 1000, 40), (12, 2049, 33)])
+def test_f64_vs_oracle_traces_and_imfs(C, L, K):
+    y = eeg(C, L, seed=C + L)
+    d = oracle.directions(C, K)
+    nimf, it = 3, 3
+    imfs, st, tr = run_gpu(y, d, nimf, it, trace=True)
+    oimfs, info = oracle.memd(y, d, nimf, it, trace=True)
+    assert np.array_equal(tr["count"], info["trace"]["count"])
+    assert np.array_equal(tr["hash"], info["trace"]["hash"])
+    for i in range(nimf):
+        assert rel_l2(imfs[i], oimfs[i]) < 1e-10, i
+    assert np.abs(imfs.sum(axis=0) - y).max() < 1e-9 * np.abs(y).max()
+
+
+def test_exact_solve_equals_windowed_solve():
+    y = eeg(8, 6000, seed=11)
+    d = oracle.directions(8, 24)
+    a, _, _ = run_gpu(y, d, 3, 4, solve_window=-1)
+    b, _, _ = run_gpu(y, d, 3, 4)
+    for i in range(3):
+        assert rel_l2(b[i], a[i]) < 1e-12
+
+
+def test_direction_chunks_do_not_change_results():
+    y = eeg(8, 3000, seed=12)
+    d = oracle.directions(8, 40)
+    a, _, _ = run_gpu(y, d, 3, 3)
+    b, _, _ = run_gpu(y, d, 3, 3, dir_chunk=16)
+    assert np.array_equal(a, b)
+
+
+def test_relaunch_is_deterministic():
+    y = eeg(4, 2500, seed=13)
+    d = oracle.directions(4, 16)
+    C, L = y.shape
+    plan = mg.Plan(C, L, 16, 4, 5)
+    dy = torch.as_tensor(y).cuda()
+    dd = torch.as_tensor(d).cuda()
+    o1 = torch.empty((4, C, L), dtype=torch.float64, device="cuda")
+    o2 = torch.empty_like(o1)
+    plan.run(dy, dd, o1)
+    plan.run(dy, dd, o2)
+    assert torch.equal(o1, o2)
+    plan.close()
+
+
+def test_no_qualified_direction_nan_and_flag():
+    y = np.tile(np.arange(64, dtype=np.float64), (2, 1))
+    d = oracle.directions(2, 4)
+    imfs, st, _ = run_gpu(y, d, 2, 1)
+    assert np.isnan(imfs[0]).all()
+    assert st.flags & mg.FLAG_NO_QUALIFIED_DIRECTION
+
+
+def test_coordinate_check():
+    y = eeg(2, 500, seed=1)
+    d = oracle.directions(2, 8)
+    good = torch.arange(500, dtype=torch.int32, device="cuda")
+    imfs, st, _ = run_gpu(y, d, 2, 2, x=good)
+    bad = good.clone()
+    bad[7] = 3
+    with pytest.raises(mg.MemdError) as ei:
+        run_gpu(y, d, 2, 2, x=bad)
+    assert ei.value.status == mg.MEMD_ERR_COORD
+
+
+def test_precision_mismatch_rejected():
+    plan = mg.Plan(2, 100, 4, 2, 1, precision=mg.PREC_F32)
+    y = torch.zeros((2, 100), dtype=torch.float64, device="cuda")
+    d = torch.zeros((4, 2), dtype=torch.float64, device="cuda")
+    o = torch.zeros((2, 2, 100), dtype=torch.float64, device="cuda")
+    st = mg.Stats()
+    rc = mg.lib().memd_run_f64(plan.handle, None, y.data_ptr(), d.data_ptr(), o.data_ptr(), None, None)
+    assert rc == mg.MEMD_ERR_PRECISION
+    plan.close()

@@ -180,6 +180,11 @@ memd_status memd_directions_f64(int64_t channels, int64_t directions, const int3
 memd_status memd_directions_f32(int64_t channels, int64_t directions, const int32_t* primes,
                                 float* d_dir, void* stream);
 
+/* Diagnostic: sustained fma throughput (flop/s, fma = 2 flops) of the current
+ * GPU for MEMD_PREC_F64 or MEMD_PREC_F32 arithmetic; the denominator of the
+ * CUDA-core roofline figures.  No reference counterpart. */
+memd_status memd_diag_fma_rate(int32_t precision, double* flops_per_s);
+
 /* Text of the last error on this thread. */
 const char* memd_last_error(void);
 /* Library version string. */

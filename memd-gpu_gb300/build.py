@@ -26,7 +26,7 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler"
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}",
             "-I/usr/local/cuda/include"]
 
-CU_SOURCES = ["memd_api.cu", "memd_directions.cu"]
+CU_SOURCES = ["memd_api.cu", "memd_directions.cu", "memd_diag.cu"]
 CXX_SOURCES = ["memd_synth.cpp"]
 
 

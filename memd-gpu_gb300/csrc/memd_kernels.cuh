@@ -335,13 +335,15 @@ k_solve(const real* __restrict__ X, const int* __restrict__ knots, const int* __
         if (i < E - 1) slope = mul_(sub_(ynext, yi), fi.ih);
         if (i > 0 && i < E - 1) r = mul_(real(3), sub_(slope, slope_prev));
         const real dcur = fmad_(-fi.lm, dprev, mul_(fi.m, r));
-        if (i < i1) {
+        // rows before i0 only warm the recurrence up: they belong to the
+        // previous segment, which writes them itself
+        if (i >= i1) {
+            halo[(i - i1) * kSolveThreads + threadIdx.x] = dcur;
+        } else if (i >= i0) {
             SY<real> v;
             v.s = dcur;
             v.y = yi;
             o[(size_t)i * C + c] = v;
-        } else {
-            halo[(i - i1) * kSolveThreads + threadIdx.x] = dcur;
         }
         slope_prev = slope;
         yi = ynext;

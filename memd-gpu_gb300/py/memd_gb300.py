@@ -34,7 +34,7 @@ TRACE_DTYPE = np.dtype([("count", "<i4"), ("flags", "<i4"), ("hash", "<u8")])
 EXPORTS = [
     "memd_default_config", "memd_plan_create", "memd_plan_destroy", "memd_plan_workspace_bytes",
     "memd_plan_set_trace", "memd_run_f64", "memd_run_f32", "memd_run_batched_f64",
-    "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_directions_f64", "memd_directions_f32", "memd_last_error",
+    "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_directions_f64", "memd_directions_f32", "memd_diag_fma_rate", "memd_last_error",
     "memd_version", "memd_synth_tones", "memd_synth_eeg", "memd_write_bin", "memd_bin_count",
     "memd_read_bin",
 ]
@@ -123,6 +123,8 @@ def lib():
         f = getattr(L, name)
         f.argtypes = [i64, i64, vp, vp, vp]
         f.restype = ctypes.c_int
+    L.memd_diag_fma_rate.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+    L.memd_diag_fma_rate.restype = ctypes.c_int
     L.memd_last_error.argtypes = []
     L.memd_last_error.restype = ctypes.c_char_p
     L.memd_version.argtypes = []
@@ -245,6 +247,13 @@ def directions(C: int, K: int, primes=None, dtype: str = "f64", out=None, stream
     fn = lib().memd_directions_f64 if dtype == "f64" else lib().memd_directions_f32
     _check(fn(C, K, None if pr is None else pr.ctypes.data_as(ctypes.c_void_p), _dptr(out), _stream_ptr(stream)))
     return out
+
+
+def fma_rate(precision: int) -> float:
+    """Measured fma throughput of the current GPU in flop/s (fma = 2 flops)."""
+    v = ctypes.c_double()
+    _check(lib().memd_diag_fma_rate(precision, ctypes.byref(v)))
+    return v.value
 
 
 def synth_eeg(C: int, L: int, fs: float = 256.0, seed: int = 0) -> np.ndarray:

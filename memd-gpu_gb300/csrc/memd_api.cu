@@ -65,6 +65,10 @@ struct memd_plan {
     void* fac;
     void* sy;
     void* rtab;
+    void* M;      // stop mode: mean envelope of the last pass [L][C]
+    void* part;   // stop mode: per channel group, direction and sample sum of (U-L)^2
+    void* amp;    // stop mode: amplitude statistic [L]
+    int egroups;  // eval channel groups
     uint32_t* bits;
     int* wpref;
     int* knots;
@@ -114,7 +118,7 @@ static void eval_launch(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
     dim3 grid((unsigned)((p->g.L + Sh::T - 1) / Sh::T), (unsigned)((p->g.C + G - 1) / G));
     k_eval<real, G, SPT><<<grid, 256, Sh::smem_bytes(p->Kc), s>>>(
         (real*)p->X, (real*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const Fac<real>*)p->fac,
-        (const SY<real>*)p->sy, p->g, k0, kc, first, last, p->st);
+        (const SY<real>*)p->sy, p->g, k0, kc, first, last, p->st, (real*)p->M, (real*)p->part);
 }
 
 #define MEMD_EVAL_CASES(X_)                                                                \
@@ -175,8 +179,11 @@ struct Launches {
 
 // ----- one sift, all direction chunks ---------------------------------------
 template <typename real>
-static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, Launches& lc)
+static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, Launches& lc,
+                         cudaGraphConditionalHandle h_sift = 0)
 {
+    const bool stop = p->cfg.stop_mode == MEMD_STOP_CRITERION;
+    const int trace_rows = stop && trace ? (int)(p->cfg.num_imfs * (p->cfg.max_iter + 1)) : 0;
     const Geom& g = p->g;
     for (int ch = 0; ch < p->nchunks; ++ch) {
         const int k0 = ch * p->Kc;
@@ -187,7 +194,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.end(MEMD_STAGE_PROJECT);
         lc.begin();
         k_compact<real><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (real*)p->yb,
-                                                           (const real*)p->X, trace, g, k0, kc, p->st);
+                                                           (const real*)p->X, trace, g, k0, kc, p->st, trace_rows);
         lc.end(MEMD_STAGE_COMPACT);
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
@@ -205,6 +212,26 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.begin();
         launch_eval<real>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
         lc.end(MEMD_STAGE_EVAL);
+        if (stop) {
+            lc.begin();
+            k_amp<real><<<(unsigned)((g.L + 255) / 256), 256, 0, s>>>((const real*)p->part, (real*)p->amp, p->cnt, g,
+                                                                    k0, kc, p->egroups, ch == 0);
+            lc.end(MEMD_STAGE_OTHER);
+        }
+    }
+    if (stop) {
+        const size_t CL = (size_t)g.C * g.L;
+        lc.begin();
+        k_stop_stats<real><<<(unsigned)std::min<long>((g.L + 255) / 256, 1024), 256, 0, s>>>(
+            (const real*)p->M, (const real*)p->amp, p->cnt, g, p->cfg.stop_sd, p->cfg.stop_sd2, p->st);
+        lc.end(MEMD_STAGE_OTHER);
+        lc.begin();
+        k_decide<<<1, 32, 0, s>>>(p->st, p->cnt, g, p->cfg.stop_tol, (int)p->cfg.max_iter, h_sift);
+        lc.end(MEMD_STAGE_OTHER);
+        lc.begin();
+        k_apply<real><<<(unsigned)std::min<size_t>((CL + 255) / 256, 4096), 256, 0, s>>>((real*)p->X,
+                                                                                        (const real*)p->M, p->st, CL);
+        lc.end(MEMD_STAGE_OTHER);
     }
 }
 
@@ -254,6 +281,95 @@ static memd_status build_graph(memd_plan* p)
     return MEMD_OK;
 }
 
+// Stop mode: the IMF loop and the sift loop are conditional WHILE nodes
+// (the sift loop nested in the IMF loop's body); k_decide and k_imf_commit set
+// their conditions on the device, so a run needs no host round trip.
+template <typename real>
+static memd_status build_graph_stop(memd_plan* p)
+{
+    if (p->exec) return MEMD_OK;
+    const Geom& g = p->g;
+    const size_t CL = (size_t)g.C * g.L;
+    const int nimf = (int)p->cfg.num_imfs;
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
+    cudaGraph_t top = nullptr;
+    cudaError_t e = cudaGraphCreate(&top, 0);
+    if (e != cudaSuccess) return set_cuda_error("graph: create", e);
+    Launches lc;
+    cudaGraphConditionalHandle h_imf = 0, h_sift = 0;
+    cudaGraphNode_t outer = nullptr, inner = nullptr;
+    cudaGraph_t obody = nullptr, ibody = nullptr;
+    std::vector<cudaGraphNode_t> d1;
+    do {
+        e = cudaGraphConditionalHandleCreate(&h_imf, top, nimf > 1 ? 1u : 0u, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) break;
+        cudaGraphNodeParams op = {};
+        op.type = cudaGraphNodeTypeConditional;
+        op.conditional.handle = h_imf;
+        op.conditional.type = cudaGraphCondTypeWhile;
+        op.conditional.size = 1;
+        e = cudaGraphAddNode(&outer, top, nullptr, nullptr, 0, &op);
+        if (e != cudaSuccess) break;
+        obody = op.conditional.phGraph_out[0];
+        e = cudaGraphConditionalHandleCreate(&h_sift, obody, 1u, 0);
+        if (e != cudaSuccess) break;
+        // IMF body, part 1: X = running residual, sift loop armed
+        e = cudaStreamBeginCaptureToGraph(p->cap, obody, nullptr, nullptr, 0, mode);
+        if (e != cudaSuccess) break;
+        cudaMemcpyAsync(p->X, p->run, CL * sizeof(real), cudaMemcpyDeviceToDevice, p->cap);
+        k_imf_begin<<<1, 32, 0, p->cap>>>(p->st, (int)p->cfg.max_iter, p->trace_dev ? 1 : 0, h_sift);
+        {
+            cudaStreamCaptureStatus cs;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            e = cudaStreamGetCaptureInfo(p->cap, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+            if (e == cudaSuccess) d1.assign(deps, deps + nd);
+        }
+        cudaGraph_t tmp = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(p->cap, &tmp);
+        if (e != cudaSuccess || e2 != cudaSuccess) { if (e == cudaSuccess) e = e2; break; }
+        cudaGraphNodeParams ip = {};
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = h_sift;
+        ip.conditional.type = cudaGraphCondTypeWhile;
+        ip.conditional.size = 1;
+        e = cudaGraphAddNode(&inner, obody, d1.data(), nullptr, d1.size(), &ip);
+        if (e != cudaSuccess) break;
+        ibody = ip.conditional.phGraph_out[0];
+        // sift body: one envelope pass + stop test + (conditional) subtraction
+        e = cudaStreamBeginCaptureToGraph(p->cap, ibody, nullptr, nullptr, 0, mode);
+        if (e != cudaSuccess) break;
+        enqueue_sift<real>(p, p->cap, p->trace_dev, lc, h_sift);
+        e = cudaStreamEndCapture(p->cap, &tmp);
+        if (e != cudaSuccess) break;
+        // IMF body, part 2: write the IMF, update the residual, continue?
+        e = cudaStreamBeginCaptureToGraph(p->cap, obody, &inner, nullptr, 1, mode);
+        if (e != cudaSuccess) break;
+        k_imf_out_dyn<real><<<tg, tb, 0, p->cap>>>((const real*)p->X, (real*)p->imf, (real*)p->run, p->st, g.C, g.L);
+        k_imf_commit<<<1, 32, 0, p->cap>>>(p->st, nimf, h_imf);
+        e = cudaStreamEndCapture(p->cap, &tmp);
+        if (e != cudaSuccess) break;
+        // after the IMF loop: unused slots zeroed, residual into the last slot
+        e = cudaStreamBeginCaptureToGraph(p->cap, top, &outer, nullptr, 1, mode);
+        if (e != cudaSuccess) break;
+        k_zero_unused<real><<<1024, 256, 0, p->cap>>>((real*)p->imf, p->st, nimf, CL);
+        k_to_channel_major<real, real><<<tg, tb, 0, p->cap>>>((const real*)p->run, (real*)p->imf + (size_t)(nimf - 1) * CL,
+                                                             nullptr, g.C, g.L);
+        e = cudaStreamEndCapture(p->cap, &tmp);
+        if (e != cudaSuccess) break;
+        e = cudaGraphInstantiate(&p->exec, top, 0);
+    } while (0);
+    cudaGraphDestroy(top);
+    if (e != cudaSuccess) {
+        p->exec = nullptr;
+        cudaGetLastError();
+        return set_cuda_error("graph: stop-mode build", e);
+    }
+    p->graph_launches = lc.count;  // kernels of one sift pass (dynamic count per run)
+    return MEMD_OK;
+}
+
 template <typename real, typename tin>
 static memd_status run_impl(memd_plan* p, const int32_t* d_x, const tin* d_y, const tin* d_dir, tin* d_imfs,
                             void* stream, memd_stats* stats)
@@ -273,7 +389,8 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const tin* d_y, co
         if (e != cudaSuccess) return set_cuda_error("run: coordinate check", e);
         if (*p->host_flag) return set_error(MEMD_ERR_COORD, "run: d_x must hold 0..L-1");
     }
-    memd_status st = build_graph<real>(p);
+    const bool stopm = p->cfg.stop_mode == MEMD_STOP_CRITERION;
+    memd_status st = stopm ? build_graph_stop<real>(p) : build_graph<real>(p);
     if (st != MEMD_OK) return st;
     cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
@@ -301,9 +418,16 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const tin* d_y, co
         memset(stats, 0, sizeof(*stats));
         stats->elapsed_ms = ms;
         stats->flags = hs.flags;
-        stats->n_imfs = (int)p->cfg.num_imfs - 1;
-        stats->launches = p->graph_launches + 1 + (d_x ? 1 : 0);
-        for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
+        if (stopm) {
+            stats->n_imfs = hs.n_imfs;
+            for (int i = 0; i < hs.n_imfs && i < 64; ++i) stats->sifts[i] = hs.sifts[i];
+            // per pass: the sift kernels; per IMF: begin, out, commit; at the end: 2
+            stats->launches = p->graph_launches * (int64_t)hs.pad[0] + 3LL * (hs.n_imfs + 1) + 2 + 1 + (d_x ? 1 : 0);
+        } else {
+            stats->n_imfs = (int)p->cfg.num_imfs - 1;
+            stats->launches = p->graph_launches + 1 + (d_x ? 1 : 0);
+            for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
+        }
     }
     return MEMD_OK;
 }
@@ -331,7 +455,31 @@ static memd_status profile_impl(memd_plan* p, const real* d_y, const real* d_dir
     cudaMemcpyAsync(p->dir, d_dir, sizeof(real) * (size_t)g.K * g.C, cudaMemcpyDeviceToDevice, s);
     memd_trace_entry* keep = p->trace_dev;
     p->trace_dev = nullptr;
-    enqueue_decomposition<real>(p, s, lc);
+    if (p->cfg.stop_mode == MEMD_STOP_CRITERION) {
+        // the graph's data-dependent loops, driven from the host
+        RunState hs;
+        const int nimf = (int)p->cfg.num_imfs;
+        for (int i = 0; i + 1 < nimf; ++i) {
+            cudaMemcpyAsync(p->X, p->run, CL * sizeof(real), cudaMemcpyDeviceToDevice, s);
+            k_imf_begin<<<1, 32, 0, s>>>(p->st, (int)p->cfg.max_iter, 0, 0);
+            for (;;) {
+                enqueue_sift<real>(p, s, nullptr, lc, 0);
+                cudaMemcpyAsync(&hs, p->st, sizeof(RunState), cudaMemcpyDeviceToHost, s);
+                cudaStreamSynchronize(s);
+                if (!hs.pad[1]) break;
+            }
+            k_imf_out_dyn<real><<<tg, tb, 0, s>>>((const real*)p->X, (real*)p->imf, (real*)p->run, p->st, g.C, g.L);
+            k_imf_commit<<<1, 32, 0, s>>>(p->st, nimf, 0);
+            cudaMemcpyAsync(&hs, p->st, sizeof(RunState), cudaMemcpyDeviceToHost, s);
+            cudaStreamSynchronize(s);
+            if (!hs.pad[2]) break;
+        }
+        k_zero_unused<real><<<1024, 256, 0, s>>>((real*)p->imf, p->st, nimf, CL);
+        k_to_channel_major<real, real><<<tg, tb, 0, s>>>((const real*)p->run, (real*)p->imf + (size_t)(nimf - 1) * CL,
+                                                         nullptr, g.C, g.L);
+    } else {
+        enqueue_decomposition<real>(p, s, lc);
+    }
     p->trace_dev = keep;
     cudaMemcpyAsync(d_imfs, p->imf, sizeof(real) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
     cudaError_t e = cudaStreamSynchronize(s);
@@ -393,7 +541,10 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     if (c.num_imfs < 1 || c.num_imfs > 4096) return set_error(MEMD_ERR_INVALID, "plan: num_imfs must be in [1, 4096]");
     if (c.max_iter < 0 || c.max_iter > 100000) return set_error(MEMD_ERR_INVALID, "plan: max_iter must be in [0, 100000]");
     if (c.precision < MEMD_PREC_F64 || c.precision > MEMD_PREC_MIXED) return set_error(MEMD_ERR_INVALID, "plan: bad precision");
-    if (c.stop_mode != MEMD_STOP_FIXED) return set_error(MEMD_ERR_UNSUPPORTED, "plan: stop criterion not built in this library");
+    if (c.stop_mode != MEMD_STOP_FIXED && c.stop_mode != MEMD_STOP_CRITERION)
+        return set_error(MEMD_ERR_INVALID, "plan: bad stop mode");
+    if (c.stop_mode == MEMD_STOP_CRITERION && (c.max_iter < 1 || !(c.stop_sd > 0) || !(c.stop_sd2 > 0) || c.stop_tol < 0))
+        return set_error(MEMD_ERR_INVALID, "plan: stop criterion needs max_iter >= 1 and positive thresholds");
     memd_plan* p = new memd_plan();  // value-initialised: every pointer and count starts at zero
     p->cfg = c;
     const int C = (int)c.channels, L = (int)c.length, K = (int)c.directions;
@@ -461,6 +612,12 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
     ALLOC(p->sy, rb * 2 * 2 * Kc * p->g.cap * C);
     ALLOC(p->rtab, rb * (size_t)(L + 1));
+    p->egroups = (C + p->evalG - 1) / p->evalG;
+    if (c.stop_mode == MEMD_STOP_CRITERION) {
+        ALLOC(p->M, rb * CL);
+        ALLOC(p->part, rb * (size_t)p->egroups * Kc * L);
+        ALLOC(p->amp, rb * (size_t)L);
+    }
     ALLOC(p->st, sizeof(RunState));
     ALLOC(p->coord_bad, sizeof(int));
 #undef ALLOC

@@ -37,15 +37,19 @@ struct Geom {
 
 // Per-run device state (counters and sticky flags).
 struct RunState {
-    int flags;          // MEMD_FLAG_* bits
-    int n_imfs;         // IMFs extracted
-    int sifts[64];      // sifts per IMF
-    int active;         // stop mode: 1 while the current IMF keeps sifting
-    int imf_active;     // stop mode: 1 while IMFs are still being extracted
-    int nbit;           // stop mode: sifts applied to the current IMF
-    int over1, over2;   // stop mode: samples above sd / sd2 in the last pass
-    int q;              // qualified directions of the last pass
-    int pad[6];
+    int flags;                 // MEMD_FLAG_* bits
+    int n_imfs;                // IMFs written so far
+    int sifts[64];             // sifts per IMF
+    int nbit;                  // stop mode: sifts applied to the current IMF
+    int pass;                  // stop mode: envelope passes of the current IMF
+    int imf_done;              // stop mode: the residual has too few extrema
+    int apply;                 // stop mode: subtract the mean of the last pass
+    unsigned long long over1;  // stop mode: samples with sigma > sd in the last pass
+    unsigned long long over2;  // stop mode: samples with sigma > sd2 in the last pass
+    int q;                     // qualified directions of the last pass
+    int trace_row;             // stop mode: trace row of the current pass (-1: none)
+    int pad[4];                // [0] passes over the run, [1] sift loop continues,
+                               // [2] IMF loop continues (mirrors of the graph conditions)
 };
 
 __device__ __forceinline__ uint64_t splitmix64(uint64_t z)

@@ -127,8 +127,15 @@ template <typename real>
 __global__ void __launch_bounds__(512)
 k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __restrict__ knots,
           int* __restrict__ cnt, real* __restrict__ yb, const real* __restrict__ X,
-          memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st)
+          memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st, int trace_rows)
 {
+    // trace_rows > 0: trace is the base of a [trace_rows][K][2] array and the
+    // row of this pass is st->trace_row (stop mode); otherwise trace points at
+    // this pass's [K][2] block.
+    if (trace && trace_rows > 0) {
+        const int r = st->trace_row;
+        trace = (r >= 0 && r < trace_rows) ? trace + (size_t)r * g.K * 2 : nullptr;
+    }
     const int env = blockIdx.x / Kc, kk = blockIdx.x - env * Kc;
     const size_t slot = (size_t)env * Kc + kk;
     const uint32_t* b = bits + slot * g.W;
@@ -388,8 +395,12 @@ __global__ void __launch_bounds__(256)
 k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restrict__ bits,
        const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
        const Fac<real>* __restrict__ fac, const SY<real>* __restrict__ sy, Geom g, int k0, int Kc,
-       int first_chunk, int last_chunk, RunState* st)
+       int first_chunk, int last_chunk, RunState* st, real* __restrict__ M, real* __restrict__ part)
 {
+    // M == nullptr: fixed mode, the last chunk updates X in place.
+    // M != nullptr: stop mode, the last chunk writes the mean envelope to M and
+    // every chunk writes part[cg][kk][n] = sum over this CTA's channels of
+    // (U - L)^2 for the amplitude statistic.
     using Sh = EvalShape<real, G, SPT>;
     constexpr int T = Sh::T;
     constexpr int MI = Sh::MI;
@@ -511,15 +522,30 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
                         const real tt = tts[t];
                         const real* cf = coef + (size_t)li * 4 * G + cc;
                         const real v = fmad_(fmad_(fmad_(cf[3 * G], tt, cf[2 * G]), tt, cf[G]), tt, cf[0]);
-                        if (env == 0) u[j] = v;
-                        else acc[j] = add_(acc[j], add_(u[j], v));
+                        if (env == 0) {
+                            u[j] = v;
+                        } else {
+                            acc[j] = add_(acc[j], add_(u[j], v));
+                            if (M) u[j] = sub_(u[j], v);  // spread U - L for the amplitude
+                        }
                     }
+                }
+            }
+            if (M && env == 1) {
+                // sum of squared spreads over the G channels of each sample row
+#pragma unroll
+                for (int j = 0; j < SPT; ++j) {
+                    const int t = row * SPT + j;
+                    real d2 = (cok && t < nl) ? mul_(u[j], u[j]) : real(0);
+#pragma unroll
+                    for (int o = 1; o < G; o <<= 1) d2 = add_(d2, __shfl_xor_sync(kFull, d2, o));
+                    if (cc == 0 && t < nl) part[((size_t)cg * Kc + kk) * g.L + n0 + t] = d2;
                 }
             }
         }
     }
     const int Q = sQ[0];
-    if (last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
+    if (!M && last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
     if (!cok) return;
 #pragma unroll
     for (int j = 0; j < SPT; ++j) {
@@ -528,12 +554,192 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
             const size_t idx = (size_t)(n0 + t) * C + c;
             if (last_chunk) {
                 const real val = mul_(acc[j], real(0.5));
-                X[idx] = sub_(X[idx], div_(val, real(Q)));
+                if (M) M[idx] = div_(val, real(Q));
+                else X[idx] = sub_(X[idx], div_(val, real(Q)));
             } else {
                 acc_buf[idx] = acc[j];
             }
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Stop mode (the sifting criterion of Rilling et al. 2003 used by Rehman &
+// Mandic 2010; no counterpart in the reference, which runs max_iter sifts).
+// ---------------------------------------------------------------------------
+// amp[n] (+)= sum over qualified directions of the chunk of
+//             sqrt(sum over channel groups of part[g][kk][n]) / 2
+template <typename real>
+__global__ void k_amp(const real* __restrict__ part, real* __restrict__ amp, const int* __restrict__ cnt,
+                      Geom g, int k0, int Kc, int groups, int first_chunk)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.L; n += gridDim.x * blockDim.x) {
+        real a = first_chunk ? real(0) : amp[n];
+        for (int kk = 0; kk < Kc; ++kk) {
+            const int k = k0 + kk;
+            if (!(cnt[k] > 3 && cnt[g.K + k] > 3)) continue;
+            real s2 = real(0);
+            for (int q = 0; q < groups; ++q) s2 = add_(s2, part[((size_t)q * Kc + kk) * g.L + n]);
+            a = fmad_(sqrt(s2), real(0.5), a);
+        }
+        amp[n] = a;
+    }
+}
+
+// sigma(n) = ||m(n)||_2 / (amp(n) / Q); counts samples above sd and sd2.
+template <typename real>
+__global__ void __launch_bounds__(256)
+k_stop_stats(const real* __restrict__ M, const real* __restrict__ amp, const int* __restrict__ cnt, Geom g,
+             double sd, double sd2, RunState* st)
+{
+    __shared__ int sq;
+    __shared__ unsigned long long s1, s2;
+    if (threadIdx.x < 32) {
+        int q = 0;
+        for (int k = threadIdx.x; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        q = warp_sum(q);
+        if (threadIdx.x == 0) {
+            sq = q;
+            s1 = 0;
+            s2 = 0;
+        }
+    }
+    __syncthreads();
+    const int Q = sq;
+    unsigned long long c1 = 0, c2 = 0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.L; n += gridDim.x * blockDim.x) {
+        real m2 = real(0);
+        for (int c = 0; c < g.C; ++c) {
+            const real v = M[(size_t)n * g.C + c];
+            m2 = fmad_(v, v, m2);
+        }
+        const real a = div_(amp[n], real(Q));
+        real sig;
+        if (a > real(0)) sig = div_(sqrt(m2), a);
+        else sig = m2 > real(0) ? real(INFINITY) : real(0);
+        c1 += ((double)sig > sd) ? 1 : 0;
+        c2 += ((double)sig > sd2) ? 1 : 0;
+    }
+    c1 = warp_sum<unsigned long long>(c1);
+    c2 = warp_sum<unsigned long long>(c2);
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&s1, c1);
+        atomicAdd(&s2, c2);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(&st->over1, s1);
+        atomicAdd(&st->over2, s2);
+    }
+}
+
+// After each pass: stop, or subtract the mean and sift again.  Before the
+// first subtraction of an IMF, a residual whose every direction has fewer
+// than 3 interior extrema ends the decomposition.  Drives the sift loop's
+// conditional WHILE node.
+__global__ void k_decide(RunState* st, const int* __restrict__ cnt, Geom g, double tol, int max_iter,
+                         cudaGraphConditionalHandle h_sift)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int q = 0;
+    bool few = true;
+    for (int k = 0; k < g.K; ++k) {
+        const int a = cnt[k], b = cnt[g.K + k];
+        if (a > 3 && b > 3) ++q;
+        if ((a - 2) + (b - 2) >= 3) few = false;
+    }
+    st->q = q;
+    unsigned cont = 0;
+    st->apply = 0;
+    if (st->pass == 0 && few) {
+        st->imf_done = 1;
+    } else {
+        const bool stop = (q == 0) || !(((double)st->over1 / (double)g.L > tol) || st->over2 > 0);
+        if (!stop) {
+            st->apply = 1;
+            st->nbit += 1;
+            cont = st->nbit < max_iter ? 1u : 0u;
+        }
+    }
+    st->pass += 1;
+    if (st->trace_row >= 0) st->trace_row += 1;
+    st->over1 = 0;
+    st->over2 = 0;
+    st->pad[0] += 1;  // passes over the whole run
+    st->pad[1] = (int)cont;
+    if (h_sift) cudaGraphSetConditional(h_sift, cont);
+}
+
+template <typename real>
+__global__ void k_apply(real* __restrict__ X, const real* __restrict__ M, const RunState* __restrict__ st, size_t n)
+{
+    if (!st->apply) return;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        X[i] = sub_(X[i], M[i]);
+}
+
+// Start of an IMF: sift counters reset, sift loop armed.
+__global__ void k_imf_begin(RunState* st, int max_iter, int tracing, cudaGraphConditionalHandle h_sift)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    st->nbit = 0;
+    st->pass = 0;
+    st->imf_done = 0;
+    st->apply = 0;
+    st->over1 = 0;
+    st->over2 = 0;
+    st->trace_row = tracing ? st->n_imfs * (max_iter + 1) : -1;
+    st->pad[1] = 1;
+    if (h_sift) cudaGraphSetConditional(h_sift, 1u);
+}
+
+// IMF slot n_imfs = X (channel-major), run -= X; skipped when the residual
+// ended the decomposition.
+template <typename real>
+__global__ void k_imf_out_dyn(const real* __restrict__ X, real* __restrict__ imf, real* __restrict__ run,
+                              const RunState* __restrict__ st, int C, int L)
+{
+    if (st->imf_done) return;
+    __shared__ real tile[32][33];
+    real* out = imf + (size_t)st->n_imfs * C * L;
+    const int n_base = blockIdx.x * 32, c_base = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int n = n_base + r, c = c_base + threadIdx.x;
+        if (c < C && n < L) {
+            const size_t idx = (size_t)n * C + c;
+            const real v = X[idx];
+            tile[r][threadIdx.x] = v;
+            run[idx] = sub_(run[idx], v);
+        }
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int c = c_base + r, n = n_base + threadIdx.x;
+        if (c < C && n < L) out[(size_t)c * L + n] = tile[threadIdx.x][r];
+    }
+}
+
+__global__ void k_imf_commit(RunState* st, int nimf, cudaGraphConditionalHandle h_imf)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned cont = 0;
+    if (!st->imf_done) {
+        const int i = st->n_imfs;
+        if (i < 64) st->sifts[i] = st->nbit;
+        st->n_imfs = i + 1;
+        cont = (st->n_imfs < nimf - 1) ? 1u : 0u;
+    }
+    st->pad[2] = (int)cont;
+    if (h_imf) cudaGraphSetConditional(h_imf, cont);
+}
+
+// Zero the IMF slots left unused when the decomposition ended early.
+template <typename real>
+__global__ void k_zero_unused(real* __restrict__ imf, const RunState* __restrict__ st, int nimf, size_t CL)
+{
+    const size_t begin = (size_t)st->n_imfs * CL, end = (size_t)(nimf - 1) * CL;
+    for (size_t i = begin + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < end; i += (size_t)gridDim.x * blockDim.x)
+        imf[i] = real(0);
 }
 
 // ---------------------------------------------------------------------------

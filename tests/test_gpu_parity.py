@@ -157,3 +157,54 @@ def test_precision_mismatch_rejected():
     rc = mg.lib().memd_run_f64(plan.handle, None, y.data_ptr(), d.data_ptr(), o.data_ptr(), None, None)
     assert rc == mg.MEMD_ERR_PRECISION
     plan.close()
+
+
+@pytest.mark.parametrize("C,L,K,maxit", [(8, 2000, 64, 50), (3, 3000, 16, 20), (32, 4096, 24, 30)])
+def test_stop_mode_matches_oracle(C, L, K, maxit):
+    """Stop criterion (sd, sd2, tol) = (0.075, 0.75, 0.075): the same sift
+    count for every IMF, the same number of IMFs, identical extrema sets at
+    every pass, IMFs within 1e-10."""
+    y = mg.synth_tones(C, L, 1000.0, seed=C) if C == 8 else eeg(C, L, seed=L)
+    d = oracle.directions(C, K)
+    nimf = 10
+    imfs, st, tr = run_gpu(y, d, nimf, maxit, trace=True, stop_mode=mg.STOP_CRITERION)
+    oimfs, info = oracle.memd(y, d, nimf, maxit, stop_mode=True, trace=True)
+    assert st.n_imfs == info["n_imfs"]
+    assert list(st.sifts[: st.n_imfs]) == list(info["sifts"][: info["n_imfs"]])
+    assert np.array_equal(tr["count"], info["trace"]["count"])
+    assert np.array_equal(tr["hash"], info["trace"]["hash"])
+    for i in range(nimf):
+        if np.linalg.norm(oimfs[i]) == 0:
+            assert np.abs(imfs[i]).max() == 0
+        else:
+            assert rel_l2(imfs[i], oimfs[i]) < 1e-10, i
+    assert np.abs(imfs.sum(axis=0) - y).max() < 1e-9 * np.abs(y).max()
+
+
+def test_stop_mode_relaunch_and_one_slot():
+    y = eeg(4, 1500, seed=2)
+    d = oracle.directions(4, 8)
+    a, sa, _ = run_gpu(y, d, 6, 20, stop_mode=mg.STOP_CRITERION)
+    C, L = y.shape
+    plan = mg.Plan(C, L, 8, 6, 20, stop_mode=mg.STOP_CRITERION)
+    dy = torch.as_tensor(y).cuda()
+    dd = torch.as_tensor(d).cuda()
+    out = torch.empty((6, C, L), dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        s2 = plan.run(dy, dd, out)
+        assert np.array_equal(out.cpu().numpy(), a) and s2.n_imfs == sa.n_imfs
+    plan.close()
+    # a single output slot: no IMF, the residual is the input
+    one, s1, _ = run_gpu(y, d, 1, 20, stop_mode=mg.STOP_CRITERION)
+    assert np.array_equal(one[0], y) and s1.n_imfs == 0
+
+
+def test_windowed_solve_bitwise_on_eeg_record():
+    """The halo of the windowed tridiagonal solve (48 knots) is far beyond the
+    decay of the spline system's inverse: the result is the exact solve's,
+    bit for bit, on a full-length record."""
+    y = eeg(32, 30504, seed=5)
+    d = oracle.directions(32, 32)
+    a, _, _ = run_gpu(y, d, 3, 3, solve_window=-1)
+    b, _, _ = run_gpu(y, d, 3, 3)
+    assert np.array_equal(a, b)

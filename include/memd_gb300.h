@@ -97,6 +97,10 @@ typedef struct {
     double elapsed_ms;     /* device time of the decomposition (CUDA events) */
     int64_t launches;      /* kernels this library launched for the run */
     int32_t sifts[64];     /* sifts per IMF (first 64 IMFs) */
+    int32_t refined;       /* mixed precision: extremum tests re-decided in
+                              double-float because the FP32 margin was within
+                              the projection's error bound */
+    int32_t reserved;
 } memd_stats;
 
 /* Per-stage device time of one eagerly launched decomposition (every kernel

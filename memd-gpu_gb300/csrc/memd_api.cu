@@ -45,30 +45,34 @@ static int next_pow2(int v)
 using memd::Fac;
 using memd::Geom;
 using memd::RunState;
-using memd::SY;
+using memd::dd;
 
 struct memd_plan {
     memd_config cfg;
     Geom g;
-    int real_bytes;
+    int prec;
+    int real_bytes;  // spline arithmetic
+    int xbytes;      // working-signal storage
+    int tbytes;      // caller's element type
     int Kc, nchunks;
     int S, H, Sf, Hf;
     int GS, ngroups;
-    int evalG, evalSPT, evalT;
-    size_t eval_smem, proj_smem, solve_smem;
+    int evalG, evalSPT, evalT;  // FP64 evaluation tile
+    int ewG, ewSPL;             // FP32 / mixed evaluation tile
+    size_t proj_smem, solve_smem;
     void* X;
     void* run;
-    void* dir;
+    void* dir;   // FP64/FP32: K x C; mixed: high words then low words
     void* acc;
     void* imf;
-    void* yb;
+    void* yv;
+    void* sv;
     void* fac;
-    void* sy;
     void* rtab;
-    void* M;      // stop mode: mean envelope of the last pass [L][C]
-    void* part;   // stop mode: per channel group, direction and sample sum of (U-L)^2
-    void* amp;    // stop mode: amplitude statistic [L]
-    int egroups;  // eval channel groups
+    void* M;     // stop mode: mean envelope of the last pass [L][C]
+    void* part;  // stop mode: per channel group, direction and sample sum of (U-L)^2
+    void* amp;   // stop mode: amplitude statistic [L]
+    int egroups; // evaluation channel groups
     uint32_t* bits;
     int* wpref;
     int* knots;
@@ -89,6 +93,12 @@ struct memd_plan {
 
 namespace memd {
 
+// Element types of the three precision forms.
+template <int P> struct Prec;
+template <> struct Prec<MEMD_PREC_F64> { using X = double; using R = double; using T = double; };
+template <> struct Prec<MEMD_PREC_F32> { using X = float;  using R = float;  using T = float; };
+template <> struct Prec<MEMD_PREC_MIXED> { using X = float2; using R = dd; using T = float; };
+
 static memd_status dev_alloc(memd_plan* p, void** ptr, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
@@ -101,55 +111,6 @@ static memd_status dev_alloc(memd_plan* p, void** ptr, size_t bytes)
     p->allocs.push_back(*ptr);
     p->bytes += bytes;
     return MEMD_OK;
-}
-
-// ----- eval dispatch -------------------------------------------------------
-template <typename real, int G, int SPT>
-static cudaError_t eval_attr()
-{
-    const size_t smem = EvalShape<real, G, SPT>::smem_bytes(1024);
-    return cudaFuncSetAttribute(k_eval<real, G, SPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
-template <typename real, int G, int SPT>
-static void eval_launch(memd_plan* p, cudaStream_t s, int k0, int kc, int first, int last)
-{
-    using Sh = EvalShape<real, G, SPT>;
-    dim3 grid((unsigned)((p->g.L + Sh::T - 1) / Sh::T), (unsigned)((p->g.C + G - 1) / G));
-    k_eval<real, G, SPT><<<grid, 256, Sh::smem_bytes(p->Kc), s>>>(
-        (real*)p->X, (real*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const Fac<real>*)p->fac,
-        (const SY<real>*)p->sy, p->g, k0, kc, first, last, p->st, (real*)p->M, (real*)p->part);
-}
-
-#define MEMD_EVAL_CASES(X_)                                                                \
-    X_(4, 2) X_(4, 4) X_(4, 8) X_(8, 2) X_(8, 4) X_(8, 8) X_(16, 2) X_(16, 4) X_(16, 8) \
-    X_(32, 4) X_(32, 8)
-
-template <typename real>
-static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first, int last)
-{
-#define MEMD_CASE(G_, S_)                                         \
-    if (p->evalG == G_ && p->evalSPT == S_) {                     \
-        eval_launch<real, G_, S_>(p, s, k0, kc, first, last);     \
-        return;                                                   \
-    }
-    MEMD_EVAL_CASES(MEMD_CASE)
-#undef MEMD_CASE
-}
-
-template <typename real>
-static cudaError_t set_attrs(memd_plan* p)
-{
-    cudaError_t e = cudaSuccess;
-#define MEMD_CASE(G_, S_) \
-    if (p->evalG == G_ && p->evalSPT == S_) e = eval_attr<real, G_, S_>();
-    MEMD_EVAL_CASES(MEMD_CASE)
-#undef MEMD_CASE
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_project_extrema<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->proj_smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_solve<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(p->solve_smem, 1));
-    return e;
 }
 
 // ----- launch accounting / per-stage timing --------------------------------
@@ -177,97 +138,184 @@ struct Launches {
     }
 };
 
+// ----- evaluation kernels ---------------------------------------------------
+#define MEMD_EVAL_CASES(X_)                                                                \
+    X_(4, 2) X_(4, 4) X_(4, 8) X_(8, 2) X_(8, 4) X_(8, 8) X_(16, 2) X_(16, 4) X_(16, 8) \
+    X_(32, 4) X_(32, 8)
+#define MEMD_EVALW_CASES(X_) X_(4, 32) X_(8, 32) X_(16, 32) X_(32, 32) X_(4, 16) X_(8, 16) X_(16, 16)
+
+template <int P>
+static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first, int last)
+{
+    using R = typename Prec<P>::R;
+    using XT = typename Prec<P>::X;
+    const Geom& g = p->g;
+    if constexpr (P == MEMD_PREC_F64) {
+#define MEMD_CASE(G_, S_)                                                                                  \
+    if (p->evalG == G_ && p->evalSPT == S_) {                                                              \
+        using Sh = EvalShape<R, G_, S_>;                                                                   \
+        dim3 grid((unsigned)((g.L + Sh::T - 1) / Sh::T), (unsigned)((g.C + G_ - 1) / G_));                 \
+        k_eval<R, G_, S_><<<grid, 256, Sh::smem_bytes(p->Kc), s>>>(                                       \
+            (R*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const Fac<R>*)p->fac,            \
+            (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part);      \
+        return;                                                                                            \
+    }
+        MEMD_EVAL_CASES(MEMD_CASE)
+#undef MEMD_CASE
+    } else {
+        const bool stopm = p->cfg.stop_mode == MEMD_STOP_CRITERION;
+#define MEMD_CASE(G_, S_)                                                                                  \
+    if (p->ewG == G_ && p->ewSPL == S_) {                                                                  \
+        using Sh = EvalWShape<G_, S_, R>;                                                                  \
+        dim3 grid((unsigned)((g.L + Sh::T - 1) / Sh::T), (unsigned)((g.C + G_ - 1) / G_));                 \
+        if (stopm)                                                                                         \
+            k_eval_w<G_, S_, XT, R, true><<<grid, 256, Sh::smem_bytes(), s>>>(                             \
+                (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
+                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part);  \
+        else                                                                                               \
+            k_eval_w<G_, S_, XT, R, false><<<grid, 256, Sh::smem_bytes(), s>>>(                            \
+                (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
+                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, nullptr, nullptr);        \
+        return;                                                                                            \
+    }
+        MEMD_EVALW_CASES(MEMD_CASE)
+#undef MEMD_CASE
+    }
+}
+
+template <int P>
+static cudaError_t set_attrs(memd_plan* p)
+{
+    using R = typename Prec<P>::R;
+    using XT = typename Prec<P>::X;
+    cudaError_t e = cudaSuccess;
+    if constexpr (P == MEMD_PREC_F64) {
+#define MEMD_CASE(G_, S_)                                                                              \
+    if (p->evalG == G_ && p->evalSPT == S_)                                                            \
+        e = cudaFuncSetAttribute(k_eval<R, G_, S_>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                                 (int)EvalShape<R, G_, S_>::smem_bytes(p->Kc));
+        MEMD_EVAL_CASES(MEMD_CASE)
+#undef MEMD_CASE
+    } else {
+#define MEMD_CASE(G_, S_)                                                                                     \
+    if (p->ewG == G_ && p->ewSPL == S_) {                                                                     \
+        e = cudaFuncSetAttribute(k_eval_w<G_, S_, XT, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                 (int)EvalWShape<G_, S_, R>::smem_bytes());                                   \
+        if (e == cudaSuccess)                                                                                 \
+            e = cudaFuncSetAttribute(k_eval_w<G_, S_, XT, R, false>,                                          \
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,                             \
+                                     (int)EvalWShape<G_, S_, R>::smem_bytes());                               \
+    }
+        MEMD_EVALW_CASES(MEMD_CASE)
+#undef MEMD_CASE
+    }
+    if (e != cudaSuccess) return e;
+    if constexpr (P == MEMD_PREC_MIXED)
+        e = cudaFuncSetAttribute(k_project_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->proj_smem);
+    else
+        e = cudaFuncSetAttribute(k_project_extrema<R, XT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)p->proj_smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_solve<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(p->solve_smem, 1));
+    return e;
+}
+
 // ----- one sift, all direction chunks ---------------------------------------
-template <typename real>
+template <int P>
 static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, Launches& lc,
                          cudaGraphConditionalHandle h_sift = 0)
 {
+    using R = typename Prec<P>::R;
+    using XT = typename Prec<P>::X;
+    const Geom& g = p->g;
     const bool stop = p->cfg.stop_mode == MEMD_STOP_CRITERION;
     const int trace_rows = stop && trace ? (int)(p->cfg.num_imfs * (p->cfg.max_iter + 1)) : 0;
-    const Geom& g = p->g;
     for (int ch = 0; ch < p->nchunks; ++ch) {
         const int k0 = ch * p->Kc;
         const int kc = std::min(p->Kc, g.K - k0);
         dim3 pg((unsigned)((g.L + kProjTN - 1) / kProjTN), (unsigned)((kc + kProjTK - 1) / kProjTK));
         lc.begin();
-        k_project_extrema<real><<<pg, 256, p->proj_smem, s>>>((const real*)p->X, (const real*)p->dir, p->bits, g, k0, kc);
+        if constexpr (P == MEMD_PREC_MIXED)
+            k_project_mx<<<pg, 256, p->proj_smem, s>>>((const float2*)p->X, (const float*)p->dir,
+                                                       (const float*)p->dir + (size_t)g.K * g.C, p->bits, g, k0, kc, p->st);
+        else
+            k_project_extrema<R, XT><<<pg, 256, p->proj_smem, s>>>((const XT*)p->X, (const R*)p->dir, p->bits, g, k0, kc);
         lc.end(MEMD_STAGE_PROJECT);
         lc.begin();
-        k_compact<real><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (real*)p->yb,
-                                                           (const real*)p->X, trace, g, k0, kc, p->st, trace_rows);
+        k_compact<R, XT><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (R*)p->yv,
+                                                            (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows);
         lc.end(MEMD_STAGE_COMPACT);
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
         lc.begin();
-        k_factor<real><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const real*)p->rtab,
-                                                                    (Fac<real>*)p->fac, g, k0, kc, p->Sf, p->Hf);
+        k_factor<R><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
+                                                                 (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf);
         lc.end(MEMD_STAGE_FACTOR);
         const long nseg = (g.cap + p->S - 1) / p->S;
         const long ns = 2L * kc * nseg * p->ngroups * p->GS;
         lc.begin();
-        k_solve<real><<<(unsigned)((ns + kSolveThreads - 1) / kSolveThreads), kSolveThreads, p->solve_smem, s>>>(
-            (const real*)p->X, p->knots, p->cnt, (const Fac<real>*)p->fac, (const real*)p->yb, (SY<real>*)p->sy, g,
-            k0, kc, p->S, p->H, p->GS, p->ngroups);
+        k_solve<R><<<(unsigned)((ns + kSolveThreads - 1) / kSolveThreads), kSolveThreads, p->solve_smem, s>>>(
+            (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->sv, g, k0, kc, p->S, p->H, p->GS, p->ngroups);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
-        launch_eval<real>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
+        launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
         lc.end(MEMD_STAGE_EVAL);
         if (stop) {
             lc.begin();
-            k_amp<real><<<(unsigned)((g.L + 255) / 256), 256, 0, s>>>((const real*)p->part, (real*)p->amp, p->cnt, g,
-                                                                    k0, kc, p->egroups, ch == 0);
+            k_amp<R><<<(unsigned)((g.L + 255) / 256), 256, 0, s>>>((const R*)p->part, (R*)p->amp, p->cnt, g, k0, kc,
+                                                                 p->egroups, ch == 0);
             lc.end(MEMD_STAGE_OTHER);
         }
     }
     if (stop) {
         const size_t CL = (size_t)g.C * g.L;
         lc.begin();
-        k_stop_stats<real><<<(unsigned)std::min<long>((g.L + 255) / 256, 1024), 256, 0, s>>>(
-            (const real*)p->M, (const real*)p->amp, p->cnt, g, p->cfg.stop_sd, p->cfg.stop_sd2, p->st);
+        k_stop_stats<R><<<(unsigned)std::min<long>((g.L + 255) / 256, 1024), 256, 0, s>>>(
+            (const R*)p->M, (const R*)p->amp, p->cnt, g, p->cfg.stop_sd, p->cfg.stop_sd2, p->st);
         lc.end(MEMD_STAGE_OTHER);
         lc.begin();
         k_decide<<<1, 32, 0, s>>>(p->st, p->cnt, g, p->cfg.stop_tol, (int)p->cfg.max_iter, h_sift);
         lc.end(MEMD_STAGE_OTHER);
         lc.begin();
-        k_apply<real><<<(unsigned)std::min<size_t>((CL + 255) / 256, 4096), 256, 0, s>>>((real*)p->X,
-                                                                                        (const real*)p->M, p->st, CL);
+        k_apply<R, XT><<<(unsigned)std::min<size_t>((CL + 255) / 256, 4096), 256, 0, s>>>((XT*)p->X, (const R*)p->M,
+                                                                                         p->st, CL);
         lc.end(MEMD_STAGE_OTHER);
     }
 }
 
-template <typename real>
+template <int P>
 static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
 {
+    using XT = typename Prec<P>::X;
+    using T = typename Prec<P>::T;
     const Geom& g = p->g;
     const size_t CL = (size_t)g.C * g.L;
     const int nimf = (int)p->cfg.num_imfs;
     const int maxit = (int)p->cfg.max_iter;
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
     for (int i = 0; i + 1 < nimf; ++i) {
-        cudaMemcpyAsync(p->X, p->run, CL * sizeof(real), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, s);
         for (int j = 0; j < maxit; ++j) {
             memd_trace_entry* tr = p->trace_dev ? p->trace_dev + ((size_t)i * (maxit + 1) + j) * (size_t)g.K * 2 : nullptr;
-            enqueue_sift<real>(p, s, tr, lc);
+            enqueue_sift<P>(p, s, tr, lc);
         }
         lc.begin();
-        k_to_channel_major<real, real><<<tg, tb, 0, s>>>((const real*)p->X, (real*)p->imf + (size_t)i * CL,
-                                                         (real*)p->run, g.C, g.L);
+        k_to_channel_major<XT, T><<<tg, tb, 0, s>>>((const XT*)p->X, (T*)p->imf + (size_t)i * CL, (XT*)p->run, g.C, g.L);
         lc.end(MEMD_STAGE_OTHER);
     }
     lc.begin();
-    k_to_channel_major<real, real><<<tg, tb, 0, s>>>((const real*)p->run, (real*)p->imf + (size_t)(nimf - 1) * CL,
-                                                     nullptr, g.C, g.L);
+    k_to_channel_major<XT, T><<<tg, tb, 0, s>>>((const XT*)p->run, (T*)p->imf + (size_t)(nimf - 1) * CL, nullptr, g.C, g.L);
     lc.end(MEMD_STAGE_OTHER);
 }
 
-template <typename real>
+template <int P>
 static memd_status build_graph(memd_plan* p)
 {
     if (p->exec) return MEMD_OK;
     cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return set_cuda_error("graph: begin capture", e);
     Launches lc;
-    enqueue_decomposition<real>(p, p->cap, lc);
+    enqueue_decomposition<P>(p, p->cap, lc);
     p->graph_launches = lc.count;
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(p->cap, &graph);
@@ -284,9 +332,11 @@ static memd_status build_graph(memd_plan* p)
 // Stop mode: the IMF loop and the sift loop are conditional WHILE nodes
 // (the sift loop nested in the IMF loop's body); k_decide and k_imf_commit set
 // their conditions on the device, so a run needs no host round trip.
-template <typename real>
+template <int P>
 static memd_status build_graph_stop(memd_plan* p)
 {
+    using XT = typename Prec<P>::X;
+    using T = typename Prec<P>::T;
     if (p->exec) return MEMD_OK;
     const Geom& g = p->g;
     const size_t CL = (size_t)g.C * g.L;
@@ -317,7 +367,7 @@ static memd_status build_graph_stop(memd_plan* p)
         // IMF body, part 1: X = running residual, sift loop armed
         e = cudaStreamBeginCaptureToGraph(p->cap, obody, nullptr, nullptr, 0, mode);
         if (e != cudaSuccess) break;
-        cudaMemcpyAsync(p->X, p->run, CL * sizeof(real), cudaMemcpyDeviceToDevice, p->cap);
+        cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, p->cap);
         k_imf_begin<<<1, 32, 0, p->cap>>>(p->st, (int)p->cfg.max_iter, p->trace_dev ? 1 : 0, h_sift);
         {
             cudaStreamCaptureStatus cs;
@@ -328,7 +378,10 @@ static memd_status build_graph_stop(memd_plan* p)
         }
         cudaGraph_t tmp = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(p->cap, &tmp);
-        if (e != cudaSuccess || e2 != cudaSuccess) { if (e == cudaSuccess) e = e2; break; }
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (e == cudaSuccess) e = e2;
+            break;
+        }
         cudaGraphNodeParams ip = {};
         ip.type = cudaGraphNodeTypeConditional;
         ip.conditional.handle = h_sift;
@@ -340,22 +393,22 @@ static memd_status build_graph_stop(memd_plan* p)
         // sift body: one envelope pass + stop test + (conditional) subtraction
         e = cudaStreamBeginCaptureToGraph(p->cap, ibody, nullptr, nullptr, 0, mode);
         if (e != cudaSuccess) break;
-        enqueue_sift<real>(p, p->cap, p->trace_dev, lc, h_sift);
+        enqueue_sift<P>(p, p->cap, p->trace_dev, lc, h_sift);
         e = cudaStreamEndCapture(p->cap, &tmp);
         if (e != cudaSuccess) break;
         // IMF body, part 2: write the IMF, update the residual, continue?
         e = cudaStreamBeginCaptureToGraph(p->cap, obody, &inner, nullptr, 1, mode);
         if (e != cudaSuccess) break;
-        k_imf_out_dyn<real><<<tg, tb, 0, p->cap>>>((const real*)p->X, (real*)p->imf, (real*)p->run, p->st, g.C, g.L);
+        k_imf_out_dyn<XT, T><<<tg, tb, 0, p->cap>>>((const XT*)p->X, (T*)p->imf, (XT*)p->run, p->st, g.C, g.L);
         k_imf_commit<<<1, 32, 0, p->cap>>>(p->st, nimf, h_imf);
         e = cudaStreamEndCapture(p->cap, &tmp);
         if (e != cudaSuccess) break;
         // after the IMF loop: unused slots zeroed, residual into the last slot
         e = cudaStreamBeginCaptureToGraph(p->cap, top, &outer, nullptr, 1, mode);
         if (e != cudaSuccess) break;
-        k_zero_unused<real><<<1024, 256, 0, p->cap>>>((real*)p->imf, p->st, nimf, CL);
-        k_to_channel_major<real, real><<<tg, tb, 0, p->cap>>>((const real*)p->run, (real*)p->imf + (size_t)(nimf - 1) * CL,
-                                                             nullptr, g.C, g.L);
+        k_zero_unused<T><<<1024, 256, 0, p->cap>>>((T*)p->imf, p->st, nimf, CL);
+        k_to_channel_major<XT, T><<<tg, tb, 0, p->cap>>>((const XT*)p->run, (T*)p->imf + (size_t)(nimf - 1) * CL,
+                                                         nullptr, g.C, g.L);
         e = cudaStreamEndCapture(p->cap, &tmp);
         if (e != cudaSuccess) break;
         e = cudaGraphInstantiate(&p->exec, top, 0);
@@ -370,13 +423,29 @@ static memd_status build_graph_stop(memd_plan* p)
     return MEMD_OK;
 }
 
-template <typename real, typename tin>
-static memd_status run_impl(memd_plan* p, const int32_t* d_x, const tin* d_y, const tin* d_dir, tin* d_imfs,
-                            void* stream, memd_stats* stats)
+// Caller's record -> working layout; directions -> plan buffer.
+template <int P>
+static void enqueue_inputs(memd_plan* p, const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
+                           cudaStream_t s, Launches& lc)
 {
-    if (!p) return set_error(MEMD_ERR_INVALID, "run: null plan");
-    if (!d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run: null pointer");
-    if ((int)sizeof(real) != p->real_bytes) return set_error(MEMD_ERR_PRECISION, "run: plan precision differs");
+    using XT = typename Prec<P>::X;
+    using T = typename Prec<P>::T;
+    const Geom& g = p->g;
+    dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
+    lc.begin();
+    k_to_sample_major<XT, T><<<tg, tb, 0, s>>>(d_y, (XT*)p->run, g.C, g.L);
+    lc.end(MEMD_STAGE_OTHER);
+    cudaMemcpyAsync(p->dir, d_dir, sizeof(T) * (size_t)g.K * g.C, cudaMemcpyDeviceToDevice, s);
+    if constexpr (P == MEMD_PREC_MIXED)  // float directions: the low words are zero
+        cudaMemsetAsync((float*)p->dir + (size_t)g.K * g.C, 0, sizeof(float) * (size_t)g.K * g.C, s);
+}
+
+template <int P>
+static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Prec<P>::T* d_y,
+                            const typename Prec<P>::T* d_dir, typename Prec<P>::T* d_imfs, void* stream,
+                            memd_stats* stats)
+{
+    using T = typename Prec<P>::T;
     cudaStream_t s = (cudaStream_t)stream;
     const Geom& g = p->g;
     const size_t CL = (size_t)g.C * g.L;
@@ -390,17 +459,16 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const tin* d_y, co
         if (*p->host_flag) return set_error(MEMD_ERR_COORD, "run: d_x must hold 0..L-1");
     }
     const bool stopm = p->cfg.stop_mode == MEMD_STOP_CRITERION;
-    memd_status st = stopm ? build_graph_stop<real>(p) : build_graph<real>(p);
+    memd_status st = stopm ? build_graph_stop<P>(p) : build_graph<P>(p);
     if (st != MEMD_OK) return st;
     cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
-    dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
-    k_to_sample_major<real, tin><<<tg, tb, 0, s>>>(d_y, (real*)p->run, g.C, g.L);
-    cudaMemcpyAsync(p->dir, d_dir, sizeof(real) * (size_t)g.K * g.C, cudaMemcpyDeviceToDevice, s);
+    Launches lc;
+    enqueue_inputs<P>(p, d_y, d_dir, s, lc);
     cudaEventRecord(p->e0, s);
     e = cudaGraphLaunch(p->exec, s);
     if (e != cudaSuccess) return set_cuda_error("run: graph launch", e);
     cudaEventRecord(p->e1, s);
-    cudaMemcpyAsync(d_imfs, p->imf, sizeof(real) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d_imfs, p->imf, sizeof(T) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
     if (p->trace_dev && p->trace_host)
         cudaMemcpyAsync(p->trace_host, p->trace_dev, sizeof(memd_trace_entry) * p->trace_n, cudaMemcpyDeviceToHost, s);
     e = cudaGetLastError();
@@ -422,22 +490,23 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const tin* d_y, co
             stats->n_imfs = hs.n_imfs;
             for (int i = 0; i < hs.n_imfs && i < 64; ++i) stats->sifts[i] = hs.sifts[i];
             // per pass: the sift kernels; per IMF: begin, out, commit; at the end: 2
-            stats->launches = p->graph_launches * (int64_t)hs.pad[0] + 3LL * (hs.n_imfs + 1) + 2 + 1 + (d_x ? 1 : 0);
+            stats->launches = p->graph_launches * (int64_t)hs.pad[0] + 3LL * (hs.n_imfs + 1) + 2 + lc.count + (d_x ? 1 : 0);
         } else {
             stats->n_imfs = (int)p->cfg.num_imfs - 1;
-            stats->launches = p->graph_launches + 1 + (d_x ? 1 : 0);
+            stats->launches = p->graph_launches + lc.count + (d_x ? 1 : 0);
             for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
         }
+        stats->refined = hs.pad[3];
     }
     return MEMD_OK;
 }
 
-template <typename real>
-static memd_status profile_impl(memd_plan* p, const real* d_y, const real* d_dir, real* d_imfs, void* stream,
-                                memd_profile* prof)
+template <int P>
+static memd_status profile_impl(memd_plan* p, const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
+                                typename Prec<P>::T* d_imfs, void* stream, memd_profile* prof)
 {
-    if (!p || !d_y || !d_dir || !d_imfs || !prof) return set_error(MEMD_ERR_INVALID, "profile: null argument");
-    if ((int)sizeof(real) != p->real_bytes) return set_error(MEMD_ERR_PRECISION, "profile: plan precision differs");
+    using XT = typename Prec<P>::X;
+    using T = typename Prec<P>::T;
     cudaStream_t s = (cudaStream_t)stream;
     const Geom& g = p->g;
     const size_t CL = (size_t)g.C * g.L;
@@ -449,10 +518,7 @@ static memd_status profile_impl(memd_plan* p, const real* d_y, const real* d_dir
     cudaEventCreate(&lc.b);
     cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
-    lc.begin();
-    k_to_sample_major<real, real><<<tg, tb, 0, s>>>(d_y, (real*)p->run, g.C, g.L);
-    lc.end(MEMD_STAGE_OTHER);
-    cudaMemcpyAsync(p->dir, d_dir, sizeof(real) * (size_t)g.K * g.C, cudaMemcpyDeviceToDevice, s);
+    enqueue_inputs<P>(p, d_y, d_dir, s, lc);
     memd_trace_entry* keep = p->trace_dev;
     p->trace_dev = nullptr;
     if (p->cfg.stop_mode == MEMD_STOP_CRITERION) {
@@ -460,28 +526,28 @@ static memd_status profile_impl(memd_plan* p, const real* d_y, const real* d_dir
         RunState hs;
         const int nimf = (int)p->cfg.num_imfs;
         for (int i = 0; i + 1 < nimf; ++i) {
-            cudaMemcpyAsync(p->X, p->run, CL * sizeof(real), cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, s);
             k_imf_begin<<<1, 32, 0, s>>>(p->st, (int)p->cfg.max_iter, 0, 0);
             for (;;) {
-                enqueue_sift<real>(p, s, nullptr, lc, 0);
+                enqueue_sift<P>(p, s, nullptr, lc, 0);
                 cudaMemcpyAsync(&hs, p->st, sizeof(RunState), cudaMemcpyDeviceToHost, s);
                 cudaStreamSynchronize(s);
                 if (!hs.pad[1]) break;
             }
-            k_imf_out_dyn<real><<<tg, tb, 0, s>>>((const real*)p->X, (real*)p->imf, (real*)p->run, p->st, g.C, g.L);
+            k_imf_out_dyn<XT, T><<<tg, tb, 0, s>>>((const XT*)p->X, (T*)p->imf, (XT*)p->run, p->st, g.C, g.L);
             k_imf_commit<<<1, 32, 0, s>>>(p->st, nimf, 0);
             cudaMemcpyAsync(&hs, p->st, sizeof(RunState), cudaMemcpyDeviceToHost, s);
             cudaStreamSynchronize(s);
             if (!hs.pad[2]) break;
         }
-        k_zero_unused<real><<<1024, 256, 0, s>>>((real*)p->imf, p->st, nimf, CL);
-        k_to_channel_major<real, real><<<tg, tb, 0, s>>>((const real*)p->run, (real*)p->imf + (size_t)(nimf - 1) * CL,
-                                                         nullptr, g.C, g.L);
+        k_zero_unused<T><<<1024, 256, 0, s>>>((T*)p->imf, p->st, nimf, CL);
+        k_to_channel_major<XT, T><<<tg, tb, 0, s>>>((const XT*)p->run, (T*)p->imf + (size_t)(nimf - 1) * CL, nullptr,
+                                                    g.C, g.L);
     } else {
-        enqueue_decomposition<real>(p, s, lc);
+        enqueue_decomposition<P>(p, s, lc);
     }
     p->trace_dev = keep;
-    cudaMemcpyAsync(d_imfs, p->imf, sizeof(real) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(d_imfs, p->imf, sizeof(T) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
     cudaError_t e = cudaStreamSynchronize(s);
     cudaEventDestroy(lc.a);
     cudaEventDestroy(lc.b);
@@ -548,7 +614,11 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     memd_plan* p = new memd_plan();  // value-initialised: every pointer and count starts at zero
     p->cfg = c;
     const int C = (int)c.channels, L = (int)c.length, K = (int)c.directions;
-    p->real_bytes = (c.precision == MEMD_PREC_F64) ? 8 : 4;
+    p->prec = c.precision;
+    const bool f64 = c.precision == MEMD_PREC_F64;
+    p->real_bytes = (f64 || c.precision == MEMD_PREC_MIXED) ? 8 : 4;  // double, float or double-float
+    p->xbytes = f64 ? 8 : (c.precision == MEMD_PREC_MIXED ? 8 : 4);
+    p->tbytes = f64 ? 8 : 4;
     p->g.C = C;
     p->g.L = L;
     p->g.K = K;
@@ -558,7 +628,6 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     p->Kc = (c.dir_chunk > 0) ? std::min<int>((int)c.dir_chunk, K) : K;
     p->Kc = std::min(p->Kc, 1024);
     p->nchunks = (K + p->Kc - 1) / p->Kc;
-    const bool f64 = p->real_bytes == 8;
     if (c.solve_window < 0) {
         p->S = p->g.cap;
         p->H = -1;
@@ -572,7 +641,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     }
     p->GS = std::min(32, next_pow2(C));
     p->ngroups = (C + p->GS - 1) / p->GS;
-    // eval tile: G channels x T samples, enough CTAs to fill the GPU
+    // FP64 evaluation tile: G channels x T samples, enough CTAs to fill the GPU
     p->evalG = std::min(32, std::max(4, next_pow2(C)));
     {
         const int NR = 256 / p->evalG;
@@ -589,30 +658,42 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         p->evalSPT = best;
         p->evalT = bestT;
     }
+    // FP32 evaluation tile: G channel lanes x 32 samples per lane; the
+    // double-float (mixed) tile keeps half the samples per lane in registers
+    if (c.precision == MEMD_PREC_MIXED) {
+        p->ewG = std::min(16, std::max(4, next_pow2(C)));
+        p->ewSPL = 16;
+    } else {
+        p->ewG = p->evalG;
+        p->ewSPL = 32;
+    }
+    p->egroups = (C + (f64 ? p->evalG : p->ewG) - 1) / (f64 ? p->evalG : p->ewG);
     const size_t rb = (size_t)p->real_bytes;
-    p->proj_smem = rb * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2));
+    if (c.precision == MEMD_PREC_MIXED)
+        p->proj_smem = 4 * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2) + C + kProjTK);
+    else
+        p->proj_smem = rb * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2));
     p->solve_smem = p->H > 0 ? rb * (size_t)p->H * kSolveThreads : 0;
     const size_t CL = (size_t)C * L;
     const size_t Kc = (size_t)p->Kc;
     memd_status st = MEMD_OK;
-#define ALLOC(ptr, bytes)                                        \
-    do {                                                         \
+#define ALLOC(ptr, bytes)                                              \
+    do {                                                               \
         if (st == MEMD_OK) st = dev_alloc(p, (void**)&(ptr), (bytes)); \
     } while (0)
-    ALLOC(p->X, rb * CL);
-    ALLOC(p->run, rb * CL);
-    ALLOC(p->dir, rb * (size_t)K * C);
+    ALLOC(p->X, (size_t)p->xbytes * CL);
+    ALLOC(p->run, (size_t)p->xbytes * CL);
+    ALLOC(p->dir, 8 * (size_t)K * C);
     if (p->nchunks > 1) ALLOC(p->acc, rb * CL);
-    ALLOC(p->imf, rb * CL * (size_t)c.num_imfs);
+    ALLOC(p->imf, (size_t)p->tbytes * CL * (size_t)c.num_imfs);
     ALLOC(p->bits, sizeof(uint32_t) * 2 * Kc * p->g.W);
     ALLOC(p->wpref, sizeof(int) * 2 * Kc * (p->g.W + 1));
     ALLOC(p->knots, sizeof(int) * 2 * Kc * p->g.cap);
     ALLOC(p->cnt, sizeof(int) * 2 * (size_t)K);
-    ALLOC(p->yb, rb * 2 * Kc * 2 * C);
     ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
-    ALLOC(p->sy, rb * 2 * 2 * Kc * p->g.cap * C);
+    ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
+    ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->rtab, rb * (size_t)(L + 1));
-    p->egroups = (C + p->evalG - 1) / p->evalG;
     if (c.stop_mode == MEMD_STOP_CRITERION) {
         ALLOC(p->M, rb * CL);
         ALLOC(p->part, rb * (size_t)p->egroups * Kc * L);
@@ -629,19 +710,27 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&p->e0);
     if (e == cudaSuccess) e = cudaEventCreate(&p->e1);
-    if (e == cudaSuccess) e = f64 ? set_attrs<double>(p) : set_attrs<float>(p);
+    if (e == cudaSuccess) {
+        if (c.precision == MEMD_PREC_F64) e = set_attrs<MEMD_PREC_F64>(p);
+        else if (c.precision == MEMD_PREC_F32) e = set_attrs<MEMD_PREC_F32>(p);
+        else e = set_attrs<MEMD_PREC_MIXED>(p);
+    }
     if (e == cudaSuccess) {
         // reciprocal table 1/h, h = 0..L (h = 0 unused)
         double* r64 = nullptr;
         float* r32 = nullptr;
+        dd* rdd = nullptr;
         e = cudaMalloc((void**)&r64, sizeof(double) * (size_t)(L + 1));
         if (e == cudaSuccess) e = cudaMalloc((void**)&r32, sizeof(float) * (size_t)(L + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&rdd, sizeof(dd) * (size_t)(L + 1));
         if (e == cudaSuccess) {
-            k_fill_reciprocals<<<256, 256>>>(r64, r32, L + 1);
-            e = cudaMemcpy(p->rtab, f64 ? (void*)r64 : (void*)r32, rb * (size_t)(L + 1), cudaMemcpyDeviceToDevice);
+            k_fill_reciprocals<<<256, 256>>>(r64, r32, rdd, L + 1);
+            const void* src = f64 ? (void*)r64 : (c.precision == MEMD_PREC_MIXED ? (void*)rdd : (void*)r32);
+            e = cudaMemcpy(p->rtab, src, rb * (size_t)(L + 1), cudaMemcpyDeviceToDevice);
         }
         cudaFree(r64);
         cudaFree(r32);
+        cudaFree(rdd);
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -677,25 +766,41 @@ memd_status memd_plan_set_trace(memd_plan* p, memd_trace_entry* host_trace)
 memd_status memd_run_f64(memd_plan* plan, const int32_t* d_x, const double* d_y, const double* d_dir,
                          double* d_imfs, void* stream, memd_stats* stats)
 {
-    return memd::run_impl<double, double>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
+    using namespace memd;
+    if (!plan) return set_error(MEMD_ERR_INVALID, "run: null plan");
+    if (!d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run: null pointer");
+    if (plan->prec != MEMD_PREC_F64) return set_error(MEMD_ERR_PRECISION, "run_f64: plan is not FP64");
+    return run_impl<MEMD_PREC_F64>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
 }
 
 memd_status memd_run_f32(memd_plan* plan, const int32_t* d_x, const float* d_y, const float* d_dir,
                          float* d_imfs, void* stream, memd_stats* stats)
 {
-    return memd::run_impl<float, float>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
+    using namespace memd;
+    if (!plan) return set_error(MEMD_ERR_INVALID, "run: null plan");
+    if (!d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run: null pointer");
+    if (plan->prec == MEMD_PREC_F32) return run_impl<MEMD_PREC_F32>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
+    if (plan->prec == MEMD_PREC_MIXED) return run_impl<MEMD_PREC_MIXED>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
+    return set_error(MEMD_ERR_PRECISION, "run_f32: plan is FP64");
 }
 
 memd_status memd_profile_f64(memd_plan* plan, const double* d_y, const double* d_dir, double* d_imfs,
                              void* stream, memd_profile* prof)
 {
-    return memd::profile_impl<double>(plan, d_y, d_dir, d_imfs, stream, prof);
+    using namespace memd;
+    if (!plan || !d_y || !d_dir || !d_imfs || !prof) return set_error(MEMD_ERR_INVALID, "profile: null argument");
+    if (plan->prec != MEMD_PREC_F64) return set_error(MEMD_ERR_PRECISION, "profile_f64: plan is not FP64");
+    return profile_impl<MEMD_PREC_F64>(plan, d_y, d_dir, d_imfs, stream, prof);
 }
 
 memd_status memd_profile_f32(memd_plan* plan, const float* d_y, const float* d_dir, float* d_imfs,
                              void* stream, memd_profile* prof)
 {
-    return memd::profile_impl<float>(plan, d_y, d_dir, d_imfs, stream, prof);
+    using namespace memd;
+    if (!plan || !d_y || !d_dir || !d_imfs || !prof) return set_error(MEMD_ERR_INVALID, "profile: null argument");
+    if (plan->prec == MEMD_PREC_F32) return profile_impl<MEMD_PREC_F32>(plan, d_y, d_dir, d_imfs, stream, prof);
+    if (plan->prec == MEMD_PREC_MIXED) return profile_impl<MEMD_PREC_MIXED>(plan, d_y, d_dir, d_imfs, stream, prof);
+    return set_error(MEMD_ERR_PRECISION, "profile_f32: plan is FP64");
 }
 
 memd_status memd_run_batched_f64(memd_plan*, int32_t, const int64_t*, const int64_t*, const double*,

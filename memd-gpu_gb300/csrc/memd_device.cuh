@@ -8,13 +8,129 @@
 
 namespace memd {
 
-// Spline solution and knot value of one (direction, envelope, knot, channel):
-// written by the tridiagonal solve, read by the envelope evaluation.
-template <typename real>
-struct alignas(2 * sizeof(real)) SY {
-    real s;   // half the second derivative at the knot (the solve's unknown)
-    real y;   // knot value after the end-point clamp
+// Double-float arithmetic: a value hi + lo with |lo| <= ulp(hi)/2, ~48
+// significant bits, computed on the FP32 pipe with error-free transformations
+// (Knuth two-sum, fma two-product; Dekker 1971, Shewchuk 1997).  Every
+// operation renormalises its result.
+struct dd {
+    float hi, lo;
+    dd() = default;
+    __host__ __device__ constexpr dd(float h, float l) : hi(h), lo(l) {}
+    __device__ explicit dd(int v) : hi((float)v), lo((float)(v - (int)(float)v)) {}
+    __device__ explicit dd(float v) : hi(v), lo(0.f) {}
+    __device__ explicit dd(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
+    __device__ explicit operator double() const { return (double)hi + (double)lo; }
+    __device__ explicit operator float() const { return hi; }
 };
+__device__ __forceinline__ dd dd_renorm(float s, float e)
+{
+    const float h = __fadd_rn(s, e);
+    return dd(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ dd operator+(dd a, dd b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    return dd_renorm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
+__device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
+__device__ __forceinline__ dd operator*(dd a, dd b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return dd_renorm(p, e);
+}
+// a * t for a plain float t (exact small integers in the evaluation)
+__device__ __forceinline__ dd dd_mulf(dd a, float t)
+{
+    const float p = __fmul_rn(a.hi, t);
+    const float e = __fmaf_rn(a.lo, t, __fmaf_rn(a.hi, t, -p));
+    return dd_renorm(p, e);
+}
+__device__ __forceinline__ dd operator/(dd a, dd b)
+{
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const dd r = a - b * dd(q1, 0.f);
+    const float q2 = __fdiv_rn(r.hi, b.hi);
+    return dd_renorm(q1, q2);
+}
+__device__ __forceinline__ bool operator>(dd a, dd b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+__device__ __forceinline__ bool operator<(dd a, dd b) { return b > a; }
+__device__ __forceinline__ dd dd_sqrt(dd a)
+{
+    if (!(a.hi > 0.f)) return dd(0.f, 0.f);
+    const float r = sqrtf(a.hi);
+    const dd e = a - dd(r, 0.f) * dd(r, 0.f);
+    return dd_renorm(r, __fdiv_rn(e.hi, 2.f * r));
+}
+
+// Working-signal storage: double (FP64 path), float (FP32 path) or float2,
+// a double-float (hi + lo, |lo| <= ulp(hi)/2) carrying ~48 significant bits
+// for the mixed-precision path.  xval() is the value the spline arithmetic of
+// type real sees.
+template <typename real>
+__device__ __forceinline__ real xval(double v) { return real(v); }
+template <typename real>
+__device__ __forceinline__ real xval(float v) { return real(v); }
+template <typename real>
+__device__ __forceinline__ real xval(float2 v) { return real(v.x); }
+template <>
+__device__ __forceinline__ dd xval<dd>(float2 v) { return dd(v.x, v.y); }
+template <>
+__device__ __forceinline__ dd xval<dd>(double v) { return dd(v); }
+template <>
+__device__ __forceinline__ dd xval<dd>(float v) { return dd(v); }
+
+// x - m for the three storage types; the double-float version is an
+// error-free two-sum followed by renormalisation.
+__device__ __forceinline__ double xsub(double x, double m) { return __dsub_rn(x, m); }
+__device__ __forceinline__ float xsub(float x, float m) { return __fsub_rn(x, m); }
+__device__ __forceinline__ float2 xsub(float2 x, float m)
+{
+    const float nm = -m;
+    const float s = __fadd_rn(x.x, nm);
+    const float bb = __fsub_rn(s, x.x);
+    const float e = __fadd_rn(__fsub_rn(x.x, __fsub_rn(s, bb)), __fsub_rn(nm, bb));
+    const float lo = __fadd_rn(x.y, e);
+    const float hi = __fadd_rn(s, lo);
+    return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+// x - y for double-float operands
+__device__ __forceinline__ float2 xsub(float2 x, float2 y)
+{
+    const float s = __fsub_rn(x.x, y.x);
+    const float bb = __fsub_rn(s, x.x);
+    const float e = __fadd_rn(__fsub_rn(x.x, __fsub_rn(s, bb)), __fsub_rn(-y.x, bb));
+    const float lo = __fadd_rn(__fsub_rn(x.y, y.y), e);
+    const float hi = __fadd_rn(s, lo);
+    return make_float2(hi, __fsub_rn(lo, __fsub_rn(hi, s)));
+}
+__device__ __forceinline__ float2 xsub(float2 x, dd m)
+{
+    const dd r = dd(x.x, x.y) - m;
+    return make_float2(r.hi, r.lo);
+}
+template <typename XT> __device__ __forceinline__ XT xzero();
+template <> __device__ __forceinline__ double xzero<double>() { return 0.0; }
+template <> __device__ __forceinline__ float xzero<float>() { return 0.0f; }
+template <> __device__ __forceinline__ float2 xzero<float2>() { return make_float2(0.f, 0.f); }
+// conversions between storage and plain types
+template <typename T> __device__ __forceinline__ T xfrom(double v);
+template <> __device__ __forceinline__ double xfrom<double>(double v) { return v; }
+template <> __device__ __forceinline__ float xfrom<float>(double v) { return (float)v; }
+template <> __device__ __forceinline__ float2 xfrom<float2>(double v)
+{
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+template <typename T> __device__ __forceinline__ T xfrom(float v) { return xfrom<T>((double)v); }
+template <typename T> __device__ __forceinline__ T xfrom(float2 v);
+template <> __device__ __forceinline__ double xfrom<double>(float2 v) { return (double)v.x + (double)v.y; }
+template <> __device__ __forceinline__ float xfrom<float>(float2 v) { return v.x; }
+template <> __device__ __forceinline__ float2 xfrom<float2>(float2 v) { return v; }
 
 // Channel-independent factorisation of the natural-spline system of one
 // (direction, envelope), per knot row i (Thomas elimination without pivoting):
@@ -80,5 +196,23 @@ __device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a,
 __device__ __forceinline__ float sub_(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double div_(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ float div_(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ dd fmad_(dd a, dd b, dd c) { return a * b + c; }
+__device__ __forceinline__ dd mul_(dd a, dd b) { return a * b; }
+__device__ __forceinline__ dd add_(dd a, dd b) { return a + b; }
+__device__ __forceinline__ dd sub_(dd a, dd b) { return a - b; }
+__device__ __forceinline__ dd div_(dd a, dd b) { return a / b; }
+__device__ __forceinline__ double shfl_xor_(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ float shfl_xor_(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ dd shfl_xor_(dd v, int o)
+{
+    return dd(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+__device__ __forceinline__ double sqrt_(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float sqrt_(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ dd sqrt_(dd a) { return dd_sqrt(a); }
+// a * t + c with a plain float t
+__device__ __forceinline__ double fmat_(double a, float t, double c) { return __fma_rn(a, (double)t, c); }
+__device__ __forceinline__ float fmat_(float a, float t, float c) { return __fmaf_rn(a, t, c); }
+__device__ __forceinline__ dd fmat_(dd a, float t, dd c) { return dd_mulf(a, t) + c; }
 
 }  // namespace memd

@@ -26,8 +26,8 @@
 //   wpref[env][kk][w]               knots before word w (w <= W)
 //   knots[env][kk][i]               knot sample indices, i < E <= cap
 //   fac[env][kk][i]                 Fac<real> per knot row
-//   sy[env][kk][i][c]               SY<real> per knot and channel
-//   yb[env][kk][2][c]               clamped end-knot values
+//   yv[env][kk][i][c]               knot values (end knots clamped)
+//   sv[env][kk][i][c]               spline solution per knot and channel
 // env 0 = maxima (upper envelope), 1 = minima (lower envelope); kk indexes the
 // directions of the current chunk, counts cnt[env][k] use the global k.
 #pragma once
@@ -48,9 +48,9 @@ constexpr int kTrace = 1;
 constexpr int kProjTN = 64;
 constexpr int kProjTK = 16;
 
-template <typename real>
+template <typename real, typename XT>
 __global__ void __launch_bounds__(256)
-k_project_extrema(const real* __restrict__ X, const real* __restrict__ dir,
+k_project_extrema(const XT* __restrict__ X, const real* __restrict__ dir,
                   uint32_t* __restrict__ bits, Geom g, int k0, int Kc)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -64,7 +64,7 @@ k_project_extrema(const real* __restrict__ X, const real* __restrict__ dir,
     for (int idx = threadIdx.x; idx < (kProjTN + 2) * C; idx += blockDim.x) {
         const int r = idx / C, c = idx - r * C;
         const int n = n0 - 1 + r;
-        xs[r * ldx + c] = (n >= 0 && n < g.L) ? X[(size_t)n * C + c] : real(0);
+        xs[r * ldx + c] = (n >= 0 && n < g.L) ? xval<real>(X[(size_t)n * C + c]) : real(0);
     }
     for (int idx = threadIdx.x; idx < kProjTK * C; idx += blockDim.x) {
         const int kk = idx / C, c = idx - kk * C;
@@ -123,10 +123,10 @@ k_project_extrema(const real* __restrict__ X, const real* __restrict__ dir,
 // ---------------------------------------------------------------------------
 // Knot lists.  One CTA of 512 threads per (envelope, direction).
 // ---------------------------------------------------------------------------
-template <typename real>
+template <typename real, typename XT>
 __global__ void __launch_bounds__(512)
 k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __restrict__ knots,
-          int* __restrict__ cnt, real* __restrict__ yb, const real* __restrict__ X,
+          int* __restrict__ cnt, real* __restrict__ yv, const XT* __restrict__ X,
           memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st, int trace_rows)
 {
     // trace_rows > 0: trace is the base of a [trace_rows][K][2] array and the
@@ -203,24 +203,32 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
         trace[(size_t)(k0 + kk) * 2 + env] = e;
     }
     if (E > g.cap || E < 2) return;
-    // End-point clamp of the knot values (REF:447-486 max, 545-584 min).
-    for (int c = threadIdx.x; c < g.C; c += blockDim.x) {
-        real v0 = X[(size_t)kn[0] * g.C + c];
-        real vE = X[(size_t)kn[E - 1] * g.C + c];
+    // Knot values of every channel (contiguous per knot), then the end-point
+    // clamp of the two end knots (REF:447-486 max, 545-584 min).
+    real* y = yv + slot * (size_t)g.cap * g.C;
+    const int C = g.C;
+    for (int idx = threadIdx.x; idx < E * C; idx += blockDim.x) {
+        const int i = idx / C, c = idx - i * C;
+        y[idx] = xval<real>(X[(size_t)kn[i] * C + c]);
+    }
+    __syncthreads();  // the raw end values are written before the clamped ones replace them
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        real v0 = xval<real>(X[(size_t)kn[0] * C + c]);
+        real vE = xval<real>(X[(size_t)kn[E - 1] * C + c]);
         if (E - 1 > 4) {
-            const real v1 = X[(size_t)kn[1] * g.C + c];
-            const real v2 = X[(size_t)kn[2] * g.C + c];
+            const real v1 = xval<real>(X[(size_t)kn[1] * C + c]);
+            const real v2 = xval<real>(X[(size_t)kn[2] * C + c]);
             real slope = div_(sub_(v2, v1), real(kn[2] - kn[1]));
             real t = fmad_(-slope, real(kn[1] - kn[0]), v1);
             if (env == 0 ? (t > v0) : (t < v0)) v0 = t;
-            const real a = X[(size_t)kn[E - 3] * g.C + c];
-            const real bb = X[(size_t)kn[E - 2] * g.C + c];
+            const real a = xval<real>(X[(size_t)kn[E - 3] * C + c]);
+            const real bb = xval<real>(X[(size_t)kn[E - 2] * C + c]);
             slope = div_(sub_(bb, a), real(kn[E - 2] - kn[E - 3]));
             t = fmad_(slope, real(kn[E - 1] - kn[E - 2]), bb);
             if (env == 0 ? (t > vE) : (t < vE)) vE = t;
         }
-        yb[(slot * 2 + 0) * g.C + c] = v0;
-        yb[(slot * 2 + 1) * g.C + c] = vE;
+        y[c] = v0;
+        y[(size_t)(E - 1) * C + c] = vE;
     }
 }
 
@@ -293,9 +301,8 @@ constexpr int kSolveThreads = 128;
 
 template <typename real>
 __global__ void __launch_bounds__(kSolveThreads)
-k_solve(const real* __restrict__ X, const int* __restrict__ knots, const int* __restrict__ cnt,
-        const Fac<real>* __restrict__ fac, const real* __restrict__ yb, SY<real>* __restrict__ sy,
-        Geom g, int k0, int Kc, int S, int H, int GS, int ngroups)
+k_solve(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
+        real* __restrict__ sv, Geom g, int k0, int Kc, int S, int H, int GS, int ngroups)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     real* halo = reinterpret_cast<real*>(smem_raw);  // [max(H,0)][kSolveThreads]
@@ -319,39 +326,27 @@ k_solve(const real* __restrict__ X, const int* __restrict__ knots, const int* __
     if (c >= g.C) return;
     const int C = g.C;
     const size_t slot = (size_t)env * Kc + kk;
-    const int* x = knots + slot * g.cap;
     const Fac<real>* f = fac + slot * g.cap;
-    SY<real>* o = sy + slot * (size_t)g.cap * C;
-    const real y0b = yb[(slot * 2 + 0) * C + c];
-    const real yEb = yb[(slot * 2 + 1) * C + c];
+    const real* y = yv + slot * (size_t)g.cap * C + c;
+    real* o = sv + slot * (size_t)g.cap * C + c;
     const int is = (H < 0) ? 0 : max(0, i0 - H);
     const int ie = (H < 0) ? E : min(E, i1 + H);
-    auto Y = [&](int i) -> real {
-        return i == 0 ? y0b : (i == E - 1 ? yEb : X[(size_t)x[i] * C + c]);
-    };
-    real yi = Y(is);
+    real yi = y[(size_t)is * C];
     real slope_prev = real(0);
-    if (is > 0) slope_prev = mul_(sub_(yi, Y(is - 1)), f[is - 1].ih);
+    if (is > 0) slope_prev = mul_(sub_(yi, y[(size_t)(is - 1) * C]), f[is - 1].ih);
     real dprev = real(0);
-    real ynext = (is < E - 1) ? Y(is + 1) : real(0);
+    real ynext = (is < E - 1) ? y[(size_t)(is + 1) * C] : real(0);
     for (int i = is; i < ie; ++i) {
         const Fac<real> fi = f[i];
-        // prefetch the knot value after next while this row is processed
-        const real yafter = (i + 2 < E) ? Y(i + 2) : real(0);
+        const real yafter = (i + 2 < E) ? y[(size_t)(i + 2) * C] : real(0);
         real slope = real(0), r = real(0);
         if (i < E - 1) slope = mul_(sub_(ynext, yi), fi.ih);
         if (i > 0 && i < E - 1) r = mul_(real(3), sub_(slope, slope_prev));
         const real dcur = fmad_(-fi.lm, dprev, mul_(fi.m, r));
         // rows before i0 only warm the recurrence up: they belong to the
         // previous segment, which writes them itself
-        if (i >= i1) {
-            halo[(i - i1) * kSolveThreads + threadIdx.x] = dcur;
-        } else if (i >= i0) {
-            SY<real> v;
-            v.s = dcur;
-            v.y = yi;
-            o[(size_t)i * C + c] = v;
-        }
+        if (i >= i1) halo[(i - i1) * kSolveThreads + threadIdx.x] = dcur;
+        else if (i >= i0) o[(size_t)i * C] = dcur;
         slope_prev = slope;
         yi = ynext;
         ynext = yafter;
@@ -359,10 +354,10 @@ k_solve(const real* __restrict__ X, const int* __restrict__ knots, const int* __
     }
     real snext = real(0);
     for (int i = ie - 1; i >= i0; --i) {
-        const real d = (i >= i1) ? halo[(i - i1) * kSolveThreads + threadIdx.x] : o[(size_t)i * C + c].s;
-        const real s = fmad_(-f[i].cp, snext, d);
-        if (i < i1) o[(size_t)i * C + c].s = s;
-        snext = s;
+        const real d = (i >= i1) ? halo[(i - i1) * kSolveThreads + threadIdx.x] : o[(size_t)i * C];
+        const real sol = fmad_(-f[i].cp, snext, d);
+        if (i < i1) o[(size_t)i * C] = sol;
+        snext = sol;
     }
 }
 
@@ -394,8 +389,9 @@ template <typename real, int G, int SPT>
 __global__ void __launch_bounds__(256)
 k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restrict__ bits,
        const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
-       const Fac<real>* __restrict__ fac, const SY<real>* __restrict__ sy, Geom g, int k0, int Kc,
-       int first_chunk, int last_chunk, RunState* st, real* __restrict__ M, real* __restrict__ part)
+       const Fac<real>* __restrict__ fac, const real* __restrict__ sv, const real* __restrict__ yv, Geom g,
+       int k0, int Kc, int first_chunk, int last_chunk, RunState* st, real* __restrict__ M,
+       real* __restrict__ part)
 {
     // M == nullptr: fixed mode, the last chunk updates X in place.
     // M != nullptr: stop mode, the last chunk writes the mean envelope to M and
@@ -472,7 +468,8 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
             }
             const int* kn = knots + slot * g.cap;
             const Fac<real>* fc = fac + slot * g.cap;
-            const SY<real>* sv = sy + slot * (size_t)g.cap * C;
+            const real* svs = sv + slot * (size_t)g.cap * C;
+            const real* yvs = yv + slot * (size_t)g.cap * C;
             const uint32_t* b = bits + slot * g.W;
             __syncthreads();
             for (int j = threadIdx.x; j <= m; j += blockDim.x) kx[j] = kn[ia + j];
@@ -498,17 +495,17 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
                 const int cch = cg * G + ch;
                 if (cch < C) {
                     const int i = ia + li;
-                    const SY<real> p0 = sv[(size_t)i * C + cch];
-                    const SY<real> p1 = sv[(size_t)(i + 1) * C + cch];
+                    const real s0 = svs[(size_t)i * C + cch], s1 = svs[(size_t)(i + 1) * C + cch];
+                    const real y0 = yvs[(size_t)i * C + cch], y1 = yvs[(size_t)(i + 1) * C + cch];
                     const real h = real(kx[li + 1] - kx[li]);
                     const real ih = ihs[li];
-                    const real slope = mul_(sub_(p1.y, p0.y), ih);
-                    const real bq = fmad_(-mul_(h, third), fmad_(real(2), p0.s, p1.s), slope);
-                    const real dq = mul_(sub_(p1.s, p0.s), mul_(ih, third));
+                    const real slope = mul_(sub_(y1, y0), ih);
+                    const real bq = fmad_(-mul_(h, third), fmad_(real(2), s0, s1), slope);
+                    const real dq = mul_(sub_(s1, s0), mul_(ih, third));
                     real* cf = coef + (size_t)li * 4 * G + ch;
-                    cf[0] = p0.y;
+                    cf[0] = y0;
                     cf[G] = bq;
-                    cf[2 * G] = p0.s;
+                    cf[2 * G] = s0;
                     cf[3 * G] = dq;
                 }
             }
@@ -538,7 +535,7 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
                     const int t = row * SPT + j;
                     real d2 = (cok && t < nl) ? mul_(u[j], u[j]) : real(0);
 #pragma unroll
-                    for (int o = 1; o < G; o <<= 1) d2 = add_(d2, __shfl_xor_sync(kFull, d2, o));
+                    for (int o = 1; o < G; o <<= 1) d2 = add_(d2, shfl_xor_(d2, o));
                     if (cc == 0 && t < nl) part[((size_t)cg * Kc + kk) * g.L + n0 + t] = d2;
                 }
             }
@@ -564,6 +561,337 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
 }
 
 // ---------------------------------------------------------------------------
+// Envelope evaluation, FP32 arithmetic, one warp per direction.
+// CTA: T = (32/G)*SPL samples x G channels, 8 warps; warp w handles the
+// directions w, w+8, ... of the chunk on its own (no block barrier inside the
+// direction loop), so the load latency of one direction is covered by the
+// other warps' work.  Per (direction, envelope) a warp stages the tile's
+// knots, knot values and solutions in its shared-memory slice, then every
+// lane walks its SPL consecutive samples of one channel, recomputing the
+// cubic's coefficients when the interval changes.  The warps' partial sums
+// are added in warp order at the end (a pairwise sum over the directions).
+// X is float (FP32 path) or float2 (double-float, mixed path).
+// ---------------------------------------------------------------------------
+template <int G, int SPL, typename R>
+struct EvalWShape {
+    static constexpr int NS = 32 / G;
+    static constexpr int T = NS * SPL;
+    static constexpr int MI = T / 2 + 4;
+    static constexpr int WARPS = 8;
+    static constexpr size_t per_warp = sizeof(int) * (MI + 1) + 2 * sizeof(R) * (MI + 1) * G + sizeof(uint32_t) * (T / 32 + 1);
+    static size_t smem_bytes()
+    {
+        const size_t stage = WARPS * ((per_warp + 15) / 16 * 16);
+        const size_t red = sizeof(R) * WARPS * T * G;
+        return stage > red ? stage : red;
+    }
+};
+
+template <int G, int SPL, typename XT, typename R, bool STOPM>
+__global__ void __launch_bounds__(256)
+k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict__ bits,
+         const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
+         const R* __restrict__ rtab, const R* __restrict__ sv, const R* __restrict__ yv, Geom g,
+         int k0, int Kc, int first_chunk, int last_chunk, RunState* st, R* __restrict__ M,
+         R* __restrict__ part)
+{
+    using Sh = EvalWShape<G, SPL, R>;
+    constexpr int T = Sh::T;
+    constexpr int MI = Sh::MI;
+    constexpr int NW = T / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int sQ;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cc = lane % G, sgrp = lane / G;
+    const int n0 = blockIdx.x * T, cg = blockIdx.y;
+    const int c = cg * G + cc;
+    const bool cok = c < g.C;
+    const int nl = min(T, g.L - n0);
+    const int C = g.C;
+    const int w0 = n0 >> 5;
+    unsigned char* wb = smem_raw + (size_t)warp * ((Sh::per_warp + 15) / 16 * 16);
+    int* kx = reinterpret_cast<int*>(wb);
+    R* ys = reinterpret_cast<R*>(kx + MI + 1);
+    R* ss = ys + (MI + 1) * G;
+    uint32_t* wd = reinterpret_cast<uint32_t*>(ss + (MI + 1) * G);
+    if (warp == 0) {
+        int q = 0;
+        for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        q = warp_sum(q);
+        if (lane == 0) sQ = q;
+    }
+    R acc[SPL];
+    R u[STOPM ? SPL : 1];
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) acc[j] = R(0.0f);
+    const int s_first = sgrp * SPL;
+    const R third = R(1.0 / 3.0);
+    bool overflow = false;
+
+    for (int kk = warp; kk < Kc; kk += Sh::WARPS) {
+        const int k = k0 + kk;
+        if (!(cnt[k] > 3 && cnt[g.K + k] > 3)) continue;
+        if (cnt[k] > g.cap || cnt[g.K + k] > g.cap) continue;
+#pragma unroll
+        for (int env = 0; env < 2; ++env) {
+            const size_t slot = (size_t)env * Kc + kk;
+            const int* wp = wpref + slot * (g.W + 1);
+            const uint32_t* b = bits + slot * g.W;
+            const int cl0 = wp[w0];
+            const uint32_t myw = (lane < NW && w0 + lane < g.W) ? b[w0 + lane] : 0u;
+            // knots strictly before the tile's last sample
+            const int nlast = nl - 1;
+            int cnt_last = 0;
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                const uint32_t w = __shfl_sync(kFull, myw, q);
+                if (32 * q + 32 <= nlast) cnt_last += __popc(w);
+                else if (32 * q < nlast) cnt_last += __popc(w & ((1u << (nlast - 32 * q)) - 1u));
+            }
+            const int ia = max(cl0 - 1, 0);
+            const int ib = max(cl0 + cnt_last - 1, 0);
+            int m = ib - ia + 1;
+            if (m > MI - 1) {
+                overflow = true;
+                m = MI - 1;
+            }
+            const int* kn = knots + slot * g.cap;
+            const R* yvs = yv + slot * (size_t)g.cap * C;
+            const R* svs = sv + slot * (size_t)g.cap * C;
+            __syncwarp();
+            for (int j = lane; j <= m; j += 32) kx[j] = kn[ia + j];
+            for (int idx = lane; idx < (m + 1) * G; idx += 32) {
+                const int j = idx / G, ch = idx - j * G;
+                const int cch = cg * G + ch;
+                const size_t off = (size_t)(ia + j) * C + cch;
+                ys[idx] = cch < C ? yvs[off] : R(0.0f);
+                ss[idx] = cch < C ? svs[off] : R(0.0f);
+            }
+            if (lane < NW) wd[lane] = myw;
+            __syncwarp();
+            // knots in [n0, n0 + s_first)
+            int cntb = 0;
+#pragma unroll
+            for (int q = 0; q < NW; ++q) {
+                const uint32_t w = wd[q];
+                if (32 * q + 32 <= s_first) cntb += __popc(w);
+                else if (32 * q < s_first) cntb += __popc(w & ((1u << (s_first - 32 * q)) - 1u));
+            }
+            int cur = -1, x0 = 0;
+            R ca = R(0.0f), cb = R(0.0f), c2 = R(0.0f), cd = R(0.0f);
+#pragma unroll
+            for (int j = 0; j < SPL; ++j) {
+                const int t = s_first + j;
+                if (t < nl) {
+                    const int iv = max(cl0 + cntb - 1, 0);
+                    const int li = min(iv - ia, m - 1);
+                    if (li != cur) {
+                        cur = li;
+                        x0 = kx[li];
+                        const int h = kx[li + 1] - x0;
+                        const R y0 = ys[li * G + cc], y1 = ys[(li + 1) * G + cc];
+                        const R s0 = ss[li * G + cc], s1 = ss[(li + 1) * G + cc];
+                        const R ih = rtab[h];
+                        const R slope = mul_(sub_(y1, y0), ih);
+                        ca = y0;
+                        cb = fmad_(-mul_(R(h), third), fmad_(R(2), s0, s1), slope);
+                        c2 = s0;
+                        cd = mul_(sub_(s1, s0), mul_(ih, third));
+                    }
+                    const float tt = (float)(n0 + t - x0);
+                    const R v = fmat_(fmat_(fmat_(cd, tt, c2), tt, cb), tt, ca);
+                    if constexpr (STOPM) {
+                        if (env == 0) {
+                            u[j] = v;
+                        } else {
+                            acc[j] = add_(acc[j], add_(u[j], v));
+                            u[j] = sub_(u[j], v);
+                        }
+                    } else {
+                        acc[j] = add_(acc[j], v);
+                    }
+                }
+                cntb += (int)((wd[t >> 5] >> (t & 31)) & 1u);
+            }
+            if constexpr (STOPM) {
+                if (env == 1) {
+#pragma unroll
+                    for (int j = 0; j < SPL; ++j) {
+                        const int t = s_first + j;
+                        R d2 = (cok && t < nl) ? mul_(u[j], u[j]) : R(0.0f);
+#pragma unroll
+                        for (int o = 1; o < G; o <<= 1) d2 = add_(d2, shfl_xor_(d2, o));
+                        if (cc == 0 && t < nl) part[((size_t)cg * Kc + kk) * g.L + n0 + t] = d2;
+                    }
+                }
+            }
+        }
+    }
+    if (overflow) atomicOr(&st->flags, 2);
+    __syncthreads();
+    R* red = reinterpret_cast<R*>(smem_raw);  // [WARPS][T][G]
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) red[((size_t)warp * T + s_first + j) * G + cc] = acc[j];
+    __syncthreads();
+    const int Q = sQ;
+    if (!M && last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
+    for (int idx = threadIdx.x; idx < T * G; idx += blockDim.x) {
+        const int t = idx / G, ch = idx - t * G;
+        const int cch = cg * G + ch;
+        if (t >= nl || cch >= C) continue;
+        const size_t off = (size_t)(n0 + t) * C + cch;
+        R tot = first_chunk ? R(0.0f) : acc_buf[off];
+#pragma unroll
+        for (int w = 0; w < Sh::WARPS; ++w) tot = add_(tot, red[((size_t)w * T + t) * G + ch]);
+        if (last_chunk) {
+            const R mval = div_(mul_(tot, R(0.5f)), R(Q));
+            if (M) M[off] = mval;
+            else X[off] = xsub(X[off], mval);
+        } else {
+            acc_buf[off] = tot;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Projection + extrema for the mixed path: P = dir . X in FP32 from the high
+// words of the double-float signal, with a rigorous bound on its error
+//   |P32 - P| <= (C+2) 2^-24 sum_c |dh_c| max|xh_c| + sum_c |dl_c| max|X_c|
+// (dh, dl: high/low words of the direction).  A comparison whose FP32 margin
+// is within twice the bound is decided again on double-float projections
+// (two-product fma splitting, ~2^-44 relative), so the extrema sets are those
+// of the FP64 projection except at ties closer than that.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_dot(const float2* __restrict__ x, const float* __restrict__ dh,
+                                         const float* __restrict__ dl, int C)
+{
+    float hi = 0.f, lo = 0.f;
+    for (int c = 0; c < C; ++c) {
+        const float2 xv = x[c];
+        const float a = dh[c], al = dl[c];
+        const float p = __fmul_rn(a, xv.x);
+        float e = __fmaf_rn(a, xv.x, -p);
+        e = __fmaf_rn(a, xv.y, __fmaf_rn(al, xv.x, e));
+        const float s = __fadd_rn(hi, p);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        lo = __fadd_rn(lo, __fadd_rn(err, e));
+        hi = s;
+    }
+    const float sh = __fadd_rn(hi, lo);
+    return make_float2(sh, __fsub_rn(lo, __fsub_rn(sh, hi)));
+}
+
+__device__ __forceinline__ bool df_gt(float2 a, float2 b) { return a.x > b.x || (a.x == b.x && a.y > b.y); }
+
+__global__ void __launch_bounds__(256)
+k_project_mx(const float2* __restrict__ X, const float* __restrict__ dh_all, const float* __restrict__ dl_all,
+             uint32_t* __restrict__ bits, Geom g, int k0, int Kc, RunState* st)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int C = g.C;
+    const int ldx = C + 1;
+    float* xs = reinterpret_cast<float*>(smem_raw);        // (TN + 2) x ldx
+    float* ds = xs + (kProjTN + 2) * ldx;                  // TK x C (high words)
+    float* ps = ds + kProjTK * C;                          // TK x (TN + 2)
+    float* mx = ps + kProjTK * (kProjTN + 2);              // C: max |x| over the tile
+    float* bnd = mx + C;                                   // TK
+    const int n0 = blockIdx.x * kProjTN;
+    const int kt0 = blockIdx.y * kProjTK;
+    for (int idx = threadIdx.x; idx < (kProjTN + 2) * C; idx += blockDim.x) {
+        const int r = idx / C, c = idx - r * C;
+        const int n = n0 - 1 + r;
+        xs[r * ldx + c] = (n >= 0 && n < g.L) ? X[(size_t)n * C + c].x : 0.f;
+    }
+    for (int idx = threadIdx.x; idx < kProjTK * C; idx += blockDim.x) {
+        const int kk = idx / C, c = idx - kk * C;
+        const int k = kt0 + kk;
+        ds[idx] = (k < Kc) ? dh_all[(size_t)(k0 + k) * C + c] : 0.f;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        float m = 0.f;
+        for (int r = 0; r < kProjTN + 2; ++r) m = fmaxf(m, fabsf(xs[r * ldx + c]));
+        mx[c] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x < kProjTK) {
+        const int k = kt0 + threadIdx.x;
+        float bh = 0.f, bl = 0.f;
+        if (k < Kc) {
+            for (int c = 0; c < C; ++c) {
+                bh = __fmaf_ru(fabsf(ds[threadIdx.x * C + c]), mx[c], bh);
+                bl = __fmaf_ru(fabsf(dl_all[(size_t)(k0 + k) * C + c]), mx[c], bl);
+            }
+        }
+        // error bound of each projection, with margin for the bound's own rounding
+        bnd[threadIdx.x] = 1.01f * ((float)(C + 2) * 5.9604645e-8f * bh + 1.0000002f * bl);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int sg = warp & 1, dg = warp >> 1;
+    {
+        const int r = 1 + sg * 32 + lane;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        const float* xr = xs + r * ldx;
+        const float* d0 = ds + (dg * 4) * C;
+        for (int c = 0; c < C; ++c) {
+            const float xv = xr[c];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[j] = __fmaf_rn(xv, d0[j * C + c], acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ps[(dg * 4 + j) * (kProjTN + 2) + r] = acc[j];
+    }
+    if (warp == 0) {
+        const int side = lane >> 4, kk = lane & 15;
+        const int r = side ? kProjTN + 1 : 0;
+        float acc = 0.f;
+        const float* xr = xs + r * ldx;
+        const float* dd = ds + kk * C;
+        for (int c = 0; c < C; ++c) acc = __fmaf_rn(xr[c], dd[c], acc);
+        ps[kk * (kProjTN + 2) + r] = acc;
+    }
+    __syncthreads();
+    const int n = n0 + sg * 32 + lane;
+    const int r = 1 + sg * 32 + lane;
+    const int last = min(g.cov, g.L - 2);
+    const bool inrange = n < g.L;
+    const bool endpt = (n == 0) || (n == g.L - 1);
+    const bool interior = (n >= 1) && (n <= last);
+    const int w = (n0 >> 5) + sg;
+    int refined = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int kk = dg * 4 + j;
+        const float* pr = ps + kk * (kProjTN + 2);
+        const float p = pr[r], pl = pr[r - 1], pn = pr[r + 1];
+        bool mxf = p > pl && p > pn;
+        bool mnf = p < pl && p < pn;
+        const float thr = 2.f * bnd[kk];
+        if (interior && kt0 + kk < Kc && (fabsf(__fsub_rn(p, pl)) <= thr || fabsf(__fsub_rn(p, pn)) <= thr)) {
+            const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
+            const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
+            const float2 a = df_dot(X + (size_t)(n - 1) * C, dh, dl, C);
+            const float2 bq = df_dot(X + (size_t)n * C, dh, dl, C);
+            const float2 cq = df_dot(X + (size_t)(n + 1) * C, dh, dl, C);
+            mxf = df_gt(bq, a) && df_gt(bq, cq);
+            mnf = df_gt(a, bq) && df_gt(cq, bq);
+            ++refined;
+        }
+        const bool mxb = inrange && (endpt || (interior && mxf));
+        const bool mnb = inrange && (endpt || (interior && mnf));
+        const uint32_t wmax = __ballot_sync(kFull, mxb);
+        const uint32_t wmin = __ballot_sync(kFull, mnb);
+        if (lane == 0 && kt0 + kk < Kc && w < g.W) {
+            bits[(size_t)(kt0 + kk) * g.W + w] = wmax;
+            bits[(size_t)(Kc + kt0 + kk) * g.W + w] = wmin;
+        }
+    }
+    refined = warp_sum(refined);
+    if (lane == 0 && refined) atomicAdd(&st->pad[3], refined);
+}
+
+// ---------------------------------------------------------------------------
 // Stop mode (the sifting criterion of Rilling et al. 2003 used by Rehman &
 // Mandic 2010; no counterpart in the reference, which runs max_iter sifts).
 // ---------------------------------------------------------------------------
@@ -580,7 +908,7 @@ __global__ void k_amp(const real* __restrict__ part, real* __restrict__ amp, con
             if (!(cnt[k] > 3 && cnt[g.K + k] > 3)) continue;
             real s2 = real(0);
             for (int q = 0; q < groups; ++q) s2 = add_(s2, part[((size_t)q * Kc + kk) * g.L + n]);
-            a = fmad_(sqrt(s2), real(0.5), a);
+            a = fmad_(sqrt_(s2), real(0.5), a);
         }
         amp[n] = a;
     }
@@ -615,10 +943,10 @@ k_stop_stats(const real* __restrict__ M, const real* __restrict__ amp, const int
         }
         const real a = div_(amp[n], real(Q));
         real sig;
-        if (a > real(0)) sig = div_(sqrt(m2), a);
-        else sig = m2 > real(0) ? real(INFINITY) : real(0);
-        c1 += ((double)sig > sd) ? 1 : 0;
-        c2 += ((double)sig > sd2) ? 1 : 0;
+        if (a > real(0.0f)) sig = div_(sqrt_(m2), a);
+        else sig = m2 > real(0.0f) ? real(INFINITY) : real(0.0f);
+        c1 += (static_cast<double>(sig) > sd) ? 1 : 0;
+        c2 += (static_cast<double>(sig) > sd2) ? 1 : 0;
     }
     c1 = warp_sum<unsigned long long>(c1);
     c2 = warp_sum<unsigned long long>(c2);
@@ -670,12 +998,12 @@ __global__ void k_decide(RunState* st, const int* __restrict__ cnt, Geom g, doub
     if (h_sift) cudaGraphSetConditional(h_sift, cont);
 }
 
-template <typename real>
-__global__ void k_apply(real* __restrict__ X, const real* __restrict__ M, const RunState* __restrict__ st, size_t n)
+template <typename real, typename XT>
+__global__ void k_apply(XT* __restrict__ X, const real* __restrict__ M, const RunState* __restrict__ st, size_t n)
 {
     if (!st->apply) return;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        X[i] = sub_(X[i], M[i]);
+        X[i] = xsub(X[i], M[i]);
 }
 
 // Start of an IMF: sift counters reset, sift loop armed.
@@ -695,27 +1023,27 @@ __global__ void k_imf_begin(RunState* st, int max_iter, int tracing, cudaGraphCo
 
 // IMF slot n_imfs = X (channel-major), run -= X; skipped when the residual
 // ended the decomposition.
-template <typename real>
-__global__ void k_imf_out_dyn(const real* __restrict__ X, real* __restrict__ imf, real* __restrict__ run,
+template <typename XT, typename TO>
+__global__ void k_imf_out_dyn(const XT* __restrict__ X, TO* __restrict__ imf, XT* __restrict__ run,
                               const RunState* __restrict__ st, int C, int L)
 {
     if (st->imf_done) return;
-    __shared__ real tile[32][33];
-    real* out = imf + (size_t)st->n_imfs * C * L;
+    __shared__ XT tile[32][33];
+    TO* out = imf + (size_t)st->n_imfs * C * L;
     const int n_base = blockIdx.x * 32, c_base = blockIdx.y * 32;
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int n = n_base + r, c = c_base + threadIdx.x;
         if (c < C && n < L) {
             const size_t idx = (size_t)n * C + c;
-            const real v = X[idx];
+            const XT v = X[idx];
             tile[r][threadIdx.x] = v;
-            run[idx] = sub_(run[idx], v);
+            run[idx] = xsub(run[idx], v);
         }
     }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int c = c_base + r, n = n_base + threadIdx.x;
-        if (c < C && n < L) out[(size_t)c * L + n] = tile[threadIdx.x][r];
+        if (c < C && n < L) out[(size_t)c * L + n] = xfrom<TO>(tile[threadIdx.x][r]);
     }
 }
 
@@ -747,14 +1075,14 @@ __global__ void k_zero_unused(real* __restrict__ imf, const RunState* __restrict
 // 32 x 32 tiles through shared memory; block (32, 8).
 // ---------------------------------------------------------------------------
 // run[n][c] = (real) y[c][n]
-template <typename real, typename tin>
-__global__ void k_to_sample_major(const tin* __restrict__ y, real* __restrict__ run, int C, int L)
+template <typename XT, typename tin>
+__global__ void k_to_sample_major(const tin* __restrict__ y, XT* __restrict__ run, int C, int L)
 {
-    __shared__ real tile[32][33];
+    __shared__ XT tile[32][33];
     const int n_base = blockIdx.x * 32, c_base = blockIdx.y * 32;
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int c = c_base + r, n = n_base + threadIdx.x;
-        if (c < C && n < L) tile[r][threadIdx.x] = real(y[(size_t)c * L + n]);
+        if (c < C && n < L) tile[r][threadIdx.x] = xfrom<XT>(y[(size_t)c * L + n]);
     }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += 8) {
@@ -764,25 +1092,25 @@ __global__ void k_to_sample_major(const tin* __restrict__ y, real* __restrict__ 
 }
 
 // out[c][n] = src[n][c]; when upd != nullptr also upd[n][c] -= src[n][c]
-template <typename real, typename tout>
-__global__ void k_to_channel_major(const real* __restrict__ src, tout* __restrict__ out,
-                                   real* __restrict__ upd, int C, int L)
+template <typename XT, typename tout>
+__global__ void k_to_channel_major(const XT* __restrict__ src, tout* __restrict__ out,
+                                   XT* __restrict__ upd, int C, int L)
 {
-    __shared__ real tile[32][33];
+    __shared__ XT tile[32][33];
     const int n_base = blockIdx.x * 32, c_base = blockIdx.y * 32;
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int n = n_base + r, c = c_base + threadIdx.x;
         if (c < C && n < L) {
             const size_t idx = (size_t)n * C + c;
-            const real v = src[idx];
+            const XT v = src[idx];
             tile[r][threadIdx.x] = v;
-            if (upd) upd[idx] = sub_(upd[idx], v);
+            if (upd) upd[idx] = xsub(upd[idx], v);
         }
     }
     __syncthreads();
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int c = c_base + r, n = n_base + threadIdx.x;
-        if (c < C && n < L) out[(size_t)c * L + n] = tout(tile[threadIdx.x][r]);
+        if (c < C && n < L) out[(size_t)c * L + n] = xfrom<tout>(tile[threadIdx.x][r]);
     }
 }
 
@@ -792,11 +1120,13 @@ __global__ void k_check_coords(const int32_t* __restrict__ x, int L, int* __rest
         if (x[n] != n) atomicOr(bad, 1);
 }
 
-__global__ void k_fill_reciprocals(double* __restrict__ r64, float* __restrict__ r32, int n)
+__global__ void k_fill_reciprocals(double* __restrict__ r64, float* __restrict__ r32, dd* __restrict__ rdd, int n)
 {
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < n; h += gridDim.x * blockDim.x) {
-        r64[h] = h > 0 ? __ddiv_rn(1.0, (double)h) : 0.0;
+        const double r = h > 0 ? __ddiv_rn(1.0, (double)h) : 0.0;
+        r64[h] = r;
         r32[h] = h > 0 ? __fdiv_rn(1.0f, (float)h) : 0.0f;
+        rdd[h] = dd(r);
     }
 }
 

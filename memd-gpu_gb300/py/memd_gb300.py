@@ -73,6 +73,8 @@ class Stats(ctypes.Structure):
         ("elapsed_ms", ctypes.c_double),
         ("launches", ctypes.c_int64),
         ("sifts", ctypes.c_int32 * 64),
+        ("refined", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

@@ -208,3 +208,45 @@ def test_windowed_solve_bitwise_on_eeg_record():
     a, _, _ = run_gpu(y, d, 3, 3, solve_window=-1)
     b, _, _ = run_gpu(y, d, 3, 3)
     assert np.array_equal(a, b)
+
+
+def _as_f32_inputs(y, d):
+    y32 = np.ascontiguousarray(y, dtype=np.float32)
+    d32 = np.ascontiguousarray(d, dtype=np.float32)
+    return y32, d32, y32.astype(np.float64), d32.astype(np.float64)
+
+
+@pytest.mark.parametrize("C,L,K", [(8, 2000, 64), (32, 8192, 64)])
+def test_mixed_extrema_certified_against_fp64(C, L, K):
+    """Mixed form (double-float working signal, certified FP32 projection,
+    FP32 splines): the first sift's extrema sets equal the FP64 path's on the
+    same input, and every IMF stays within 1e-4 relative L2."""
+    y = eeg(C, L, seed=21) if C > 8 else mg.synth_tones(C, L, 1000.0, seed=3)
+    d = oracle.directions(C, K)
+    y32, d32, y64, d64 = _as_f32_inputs(y, d)
+    a, sa, ta = run_gpu(y64, d64, 6, 10, trace=True)
+    b, sb, tb = run_gpu(y32, d32, 6, 10, precision=mg.PREC_MIXED, trace=True)
+    assert np.array_equal(ta["count"][0, 0], tb["count"][0, 0])
+    assert np.array_equal(ta["hash"][0, 0], tb["hash"][0, 0])
+    for i in range(6):
+        assert rel_l2(b[i], a[i]) < 1e-4, i
+    assert sb.flags == 0
+
+
+def test_fp32_path_runs_fast_eval_and_reconstructs():
+    y = eeg(16, 5000, seed=4)
+    d = oracle.directions(16, 32)
+    y32, d32, _, _ = _as_f32_inputs(y, d)
+    imfs, st, _ = run_gpu(y32, d32, 5, 6, precision=mg.PREC_F32)
+    assert np.isfinite(imfs).all()
+    assert np.abs(imfs.astype(np.float64).sum(axis=0) - y32).max() < 1e-3 * np.abs(y32).max()
+
+
+def test_mixed_stop_mode_runs():
+    y = mg.synth_tones(8, 2000, 1000.0, seed=1)
+    d = oracle.directions(8, 64)
+    y32, d32, y64, d64 = _as_f32_inputs(y, d)
+    a, sa, _ = run_gpu(y64, d64, 10, 50, stop_mode=mg.STOP_CRITERION)
+    b, sb, _ = run_gpu(y32, d32, 10, 50, precision=mg.PREC_MIXED, stop_mode=mg.STOP_CRITERION)
+    assert sb.n_imfs >= 1
+    assert np.abs(b.astype(np.float64).sum(axis=0) - y32).max() < 1e-4 * np.abs(y32).max()

@@ -169,11 +169,11 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
         using Sh = EvalWShape<G_, S_, R>;                                                                  \
         dim3 grid((unsigned)((g.L + Sh::T - 1) / Sh::T), (unsigned)((g.C + G_ - 1) / G_));                 \
         if (stopm)                                                                                         \
-            k_eval_w<G_, S_, XT, R, true><<<grid, 256, Sh::smem_bytes(), s>>>(                             \
+            k_eval_w<G_, S_, XT, R, true><<<grid, 256, Sh::smem_bytes(true), s>>>(                         \
                 (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
                 (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part);  \
         else                                                                                               \
-            k_eval_w<G_, S_, XT, R, false><<<grid, 256, Sh::smem_bytes(), s>>>(                            \
+            k_eval_w<G_, S_, XT, R, false><<<grid, 256, Sh::smem_bytes(false), s>>>(                       \
                 (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
                 (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, nullptr, nullptr);        \
         return;                                                                                            \
@@ -200,11 +200,11 @@ static cudaError_t set_attrs(memd_plan* p)
 #define MEMD_CASE(G_, S_)                                                                                     \
     if (p->ewG == G_ && p->ewSPL == S_) {                                                                     \
         e = cudaFuncSetAttribute(k_eval_w<G_, S_, XT, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
-                                 (int)EvalWShape<G_, S_, R>::smem_bytes());                                   \
+                                 (int)EvalWShape<G_, S_, R>::smem_bytes(true));                               \
         if (e == cudaSuccess)                                                                                 \
             e = cudaFuncSetAttribute(k_eval_w<G_, S_, XT, R, false>,                                          \
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,                             \
-                                     (int)EvalWShape<G_, S_, R>::smem_bytes());                               \
+                                     (int)EvalWShape<G_, S_, R>::smem_bytes(false));                          \
     }
         MEMD_EVALW_CASES(MEMD_CASE)
 #undef MEMD_CASE
@@ -634,10 +634,13 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         p->Sf = p->g.cap;
         p->Hf = -1;
     } else {
+        // halo lengths: the truncation error decays by <= 1/2 (solve) and
+        // <= 1/3 (pivots) per knot; FP64 and double-float need ~1e-15
+        const bool wide = f64 || c.precision == MEMD_PREC_MIXED;
         p->S = 256;
-        p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : 24);
-        p->Sf = 256;
-        p->Hf = f64 ? 40 : 20;
+        p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : (wide ? 32 : 24));
+        p->Sf = 64;
+        p->Hf = wide ? 40 : 20;
     }
     p->GS = std::min(32, next_pow2(C));
     p->ngroups = (C + p->GS - 1) / p->GS;

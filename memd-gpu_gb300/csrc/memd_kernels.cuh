@@ -336,6 +336,7 @@ k_solve(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real
     if (is > 0) slope_prev = mul_(sub_(yi, y[(size_t)(is - 1) * C]), f[is - 1].ih);
     real dprev = real(0);
     real ynext = (is < E - 1) ? y[(size_t)(is + 1) * C] : real(0);
+#pragma unroll 4
     for (int i = is; i < ie; ++i) {
         const Fac<real> fi = f[i];
         const real yafter = (i + 2 < E) ? y[(size_t)(i + 2) * C] : real(0);
@@ -353,6 +354,7 @@ k_solve(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real
         dprev = dcur;
     }
     real snext = real(0);
+#pragma unroll 4
     for (int i = ie - 1; i >= i0; --i) {
         const real d = (i >= i1) ? halo[(i - i1) * kSolveThreads + threadIdx.x] : o[(size_t)i * C];
         const real sol = fmad_(-f[i].cp, snext, d);
@@ -578,13 +580,13 @@ struct EvalWShape {
     static constexpr int T = NS * SPL;
     static constexpr int MI = T / 2 + 4;
     static constexpr int WARPS = 8;
-    static constexpr size_t per_warp = sizeof(int) * (MI + 1) + 2 * sizeof(R) * (MI + 1) * G + sizeof(uint32_t) * (T / 32 + 1);
-    static size_t smem_bytes()
+    static constexpr int NW = T / 32;
+    // per warp: accumulator tile, (stop mode) spread tile, knots, bit words
+    __host__ __device__ static constexpr size_t per_warp(bool stopm)
     {
-        const size_t stage = WARPS * ((per_warp + 15) / 16 * 16);
-        const size_t red = sizeof(R) * WARPS * T * G;
-        return stage > red ? stage : red;
+        return (size_t)(stopm ? 2 : 1) * sizeof(R) * T * G + sizeof(int) * (MI + 1) + sizeof(uint32_t) * (NW + 1);
     }
+    static size_t smem_bytes(bool stopm) { return WARPS * ((per_warp(stopm) + 15) / 16 * 16); }
 };
 
 template <int G, int SPL, typename XT, typename R, bool STOPM>
@@ -598,7 +600,8 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
     using Sh = EvalWShape<G, SPL, R>;
     constexpr int T = Sh::T;
     constexpr int MI = Sh::MI;
-    constexpr int NW = T / 32;
+    constexpr int NW = Sh::NW;
+    constexpr size_t PW = (Sh::per_warp(STOPM) + 15) / 16 * 16;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int sQ;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -609,37 +612,34 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
     const int nl = min(T, g.L - n0);
     const int C = g.C;
     const int w0 = n0 >> 5;
-    unsigned char* wb = smem_raw + (size_t)warp * ((Sh::per_warp + 15) / 16 * 16);
-    int* kx = reinterpret_cast<int*>(wb);
-    R* ys = reinterpret_cast<R*>(kx + MI + 1);
-    R* ss = ys + (MI + 1) * G;
-    uint32_t* wd = reinterpret_cast<uint32_t*>(ss + (MI + 1) * G);
+    unsigned char* wb = smem_raw + (size_t)warp * PW;
+    R* accs = reinterpret_cast<R*>(wb);                        // [T][G]
+    R* us = accs + (STOPM ? T * G : 0);                        // [T][G] (stop mode)
+    int* kx = reinterpret_cast<int*>(accs + (STOPM ? 2 : 1) * T * G);
+    uint32_t* wd = reinterpret_cast<uint32_t*>(kx + MI + 1);
     if (warp == 0) {
         int q = 0;
         for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
         q = warp_sum(q);
         if (lane == 0) sQ = q;
     }
-    R acc[SPL];
-    R u[STOPM ? SPL : 1];
-#pragma unroll
-    for (int j = 0; j < SPL; ++j) acc[j] = R(0.0f);
     const int s_first = sgrp * SPL;
+    for (int j = 0; j < SPL; ++j) accs[(s_first + j) * G + cc] = R(0.0f);
     const R third = R(1.0 / 3.0);
+    const R* yc = yv + c;
+    const R* sc = sv + c;
     bool overflow = false;
 
     for (int kk = warp; kk < Kc; kk += Sh::WARPS) {
         const int k = k0 + kk;
         if (!(cnt[k] > 3 && cnt[g.K + k] > 3)) continue;
         if (cnt[k] > g.cap || cnt[g.K + k] > g.cap) continue;
-#pragma unroll
         for (int env = 0; env < 2; ++env) {
             const size_t slot = (size_t)env * Kc + kk;
             const int* wp = wpref + slot * (g.W + 1);
             const uint32_t* b = bits + slot * g.W;
             const int cl0 = wp[w0];
             const uint32_t myw = (lane < NW && w0 + lane < g.W) ? b[w0 + lane] : 0u;
-            // knots strictly before the tile's last sample
             const int nlast = nl - 1;
             int cnt_last = 0;
 #pragma unroll
@@ -656,20 +656,11 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
                 m = MI - 1;
             }
             const int* kn = knots + slot * g.cap;
-            const R* yvs = yv + slot * (size_t)g.cap * C;
-            const R* svs = sv + slot * (size_t)g.cap * C;
+            const size_t base = (slot * (size_t)g.cap + ia) * C;  // knot ia, channel 0
             __syncwarp();
             for (int j = lane; j <= m; j += 32) kx[j] = kn[ia + j];
-            for (int idx = lane; idx < (m + 1) * G; idx += 32) {
-                const int j = idx / G, ch = idx - j * G;
-                const int cch = cg * G + ch;
-                const size_t off = (size_t)(ia + j) * C + cch;
-                ys[idx] = cch < C ? yvs[off] : R(0.0f);
-                ss[idx] = cch < C ? svs[off] : R(0.0f);
-            }
             if (lane < NW) wd[lane] = myw;
             __syncwarp();
-            // knots in [n0, n0 + s_first)
             int cntb = 0;
 #pragma unroll
             for (int q = 0; q < NW; ++q) {
@@ -677,48 +668,63 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
                 if (32 * q + 32 <= s_first) cntb += __popc(w);
                 else if (32 * q < s_first) cntb += __popc(w & ((1u << (s_first - 32 * q)) - 1u));
             }
-            int cur = -1, x0 = 0;
+            int cur = -2, x0 = 0;  // -2: no interval loaded yet (li >= 0 never equals cur + 1)
             R ca = R(0.0f), cb = R(0.0f), c2 = R(0.0f), cd = R(0.0f);
-#pragma unroll
+            R ynx = R(0.0f), snx = R(0.0f);  // values at knot cur + 1
+#pragma unroll 2
             for (int j = 0; j < SPL; ++j) {
                 const int t = s_first + j;
-                if (t < nl) {
+                if (t < nl && cok) {
                     const int iv = max(cl0 + cntb - 1, 0);
                     const int li = min(iv - ia, m - 1);
                     if (li != cur) {
+                        R y0, s0;
+                        if (li == cur + 1) {
+                            y0 = ynx;
+                            s0 = snx;
+                        } else {
+                            y0 = yc[base + (size_t)li * C];
+                            s0 = sc[base + (size_t)li * C];
+                        }
+                        ynx = yc[base + (size_t)(li + 1) * C];
+                        snx = sc[base + (size_t)(li + 1) * C];
                         cur = li;
                         x0 = kx[li];
                         const int h = kx[li + 1] - x0;
-                        const R y0 = ys[li * G + cc], y1 = ys[(li + 1) * G + cc];
-                        const R s0 = ss[li * G + cc], s1 = ss[(li + 1) * G + cc];
                         const R ih = rtab[h];
-                        const R slope = mul_(sub_(y1, y0), ih);
+                        const R slope = mul_(sub_(ynx, y0), ih);
                         ca = y0;
-                        cb = fmad_(-mul_(R(h), third), fmad_(R(2), s0, s1), slope);
+                        cb = fmad_(-mul_(R(h), third), fmad_(R(2), s0, snx), slope);
                         c2 = s0;
-                        cd = mul_(sub_(s1, s0), mul_(ih, third));
+                        cd = mul_(sub_(snx, s0), mul_(ih, third));
                     }
                     const float tt = (float)(n0 + t - x0);
                     const R v = fmat_(fmat_(fmat_(cd, tt, c2), tt, cb), tt, ca);
+                    const int idx = t * G + cc;
                     if constexpr (STOPM) {
                         if (env == 0) {
-                            u[j] = v;
+                            us[idx] = v;
                         } else {
-                            acc[j] = add_(acc[j], add_(u[j], v));
-                            u[j] = sub_(u[j], v);
+                            const R uu = us[idx];
+                            accs[idx] = add_(accs[idx], add_(uu, v));
+                            us[idx] = sub_(uu, v);
                         }
                     } else {
-                        acc[j] = add_(acc[j], v);
+                        accs[idx] = add_(accs[idx], v);
                     }
                 }
                 cntb += (int)((wd[t >> 5] >> (t & 31)) & 1u);
             }
             if constexpr (STOPM) {
                 if (env == 1) {
-#pragma unroll
+                    __syncwarp();
                     for (int j = 0; j < SPL; ++j) {
                         const int t = s_first + j;
-                        R d2 = (cok && t < nl) ? mul_(u[j], u[j]) : R(0.0f);
+                        R d2 = R(0.0f);
+                        if (cok && t < nl) {
+                            const R uu = us[t * G + cc];
+                            d2 = mul_(uu, uu);
+                        }
 #pragma unroll
                         for (int o = 1; o < G; o <<= 1) d2 = add_(d2, shfl_xor_(d2, o));
                         if (cc == 0 && t < nl) part[((size_t)cg * Kc + kk) * g.L + n0 + t] = d2;
@@ -729,10 +735,6 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
     }
     if (overflow) atomicOr(&st->flags, 2);
     __syncthreads();
-    R* red = reinterpret_cast<R*>(smem_raw);  // [WARPS][T][G]
-#pragma unroll
-    for (int j = 0; j < SPL; ++j) red[((size_t)warp * T + s_first + j) * G + cc] = acc[j];
-    __syncthreads();
     const int Q = sQ;
     if (!M && last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
     for (int idx = threadIdx.x; idx < T * G; idx += blockDim.x) {
@@ -742,7 +744,8 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
         const size_t off = (size_t)(n0 + t) * C + cch;
         R tot = first_chunk ? R(0.0f) : acc_buf[off];
 #pragma unroll
-        for (int w = 0; w < Sh::WARPS; ++w) tot = add_(tot, red[((size_t)w * T + t) * G + ch]);
+        for (int w = 0; w < Sh::WARPS; ++w)
+            tot = add_(tot, reinterpret_cast<const R*>(smem_raw + (size_t)w * PW)[idx]);
         if (last_chunk) {
             const R mval = div_(mul_(tot, R(0.5f)), R(Q));
             if (M) M[off] = mval;

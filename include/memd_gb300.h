@@ -184,6 +184,21 @@ memd_status memd_directions_f64(int64_t channels, int64_t directions, const int3
 memd_status memd_directions_f32(int64_t channels, int64_t directions, const int32_t* primes,
                                 float* d_dir, void* stream);
 
+/* Same direction set as memd_directions_f64, for callers that must not
+ * allocate device memory: a MATLAB MEX function whose GPU buffers have to come
+ * from MATLAB's own allocator, a real-time acquisition loop that cannot
+ * afford the device-wide synchronisation cudaMalloc/cudaFree may cause, or an
+ * application that hands out all device memory from one arena it owns.  It
+ * allocates nothing: the prime table lives in a static device array of 4096
+ * entries, so channels > 4096 is rejected (MEMD_ERR_INVALID).  The array is
+ * shared by all calls: calls whose copies and kernels overlap on the GPU (for
+ * example on two streams) race and must be ordered by the caller.  The first
+ * call on each device looks up the array's device address; make that first
+ * call before any stream capture that includes this entry point.
+ * No counterpart in the reference (which always allocates its tables). */
+memd_status memd_directions_noalloc_f64(int64_t channels, int64_t directions, const int32_t* primes,
+                                        double* d_dir, void* stream);
+
 /* Diagnostic: sustained fma throughput (flop/s, fma = 2 flops) of the current
  * GPU for MEMD_PREC_F64 or MEMD_PREC_F32 arithmetic; the denominator of the
  * CUDA-core roofline figures.  No reference counterpart. */

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "memd_device.cuh"
@@ -107,7 +108,86 @@ static memd_status directions_impl(int64_t C, int64_t K, const int32_t* primes, 
     return MEMD_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant.  The prime table the kernel reads lives in this
+// file-scope device array instead of a per-call allocation.  The array holds
+// kNoAllocMaxChannels entries on every GPU that loads the library, until the
+// process exits.  Host code may not hand the array's name to a kernel (on the
+// host it is only a stand-in for the device symbol), so its device address is
+// looked up once per device with cudaGetSymbolAddress and cached.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocMaxChannels = 4096;
+static __device__ __align__(256) int g_noalloc_primes[kNoAllocMaxChannels];
+
+static std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 256;
+static int* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_primes on the current device; the first call on
+// a device resolves it (with that device current) and caches it.
+static memd_status noalloc_table(int** out)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_cuda_error("directions_noalloc: cudaGetDevice", e);
+    if (dev < 0 || dev >= kMaxDevices) return set_error(MEMD_ERR_INVALID, "directions_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_noalloc_primes);
+        if (e != cudaSuccess || !ptr) return set_cuda_error("directions_noalloc: cudaGetSymbolAddress", e);
+        g_noalloc_addr[dev] = static_cast<int*>(ptr);
+    }
+    *out = g_noalloc_addr[dev];
+    return MEMD_OK;
+}
+
+static memd_status directions_noalloc(int64_t C, int64_t K, const int32_t* primes, double* d_dir, void* stream)
+{
+    if (C < 1 || K < 1 || K > (1 << 20) || !d_dir) return set_error(MEMD_ERR_INVALID, "directions_noalloc: bad arguments");
+    if (C > kNoAllocMaxChannels)
+        return set_error(MEMD_ERR_INVALID,
+                         "directions_noalloc: channels exceeds the 4096-entry static prime table; use memd_directions_f64");
+    // the table is built on the stack: no heap or device allocation anywhere
+    int table[kNoAllocMaxChannels];
+    if (primes) {
+        for (int64_t c = 0; c < C; ++c) table[c] = primes[c];
+    } else {
+        int cnt = 1, cand = 2;
+        while (cnt < C) {
+            bool composite = false;
+            for (int d = 2; d <= cand / 2; ++d)
+                if (cand % d == 0) { composite = true; break; }
+            if (!composite) table[cnt++] = cand;
+            ++cand;
+        }
+        table[0] = -(int)K;
+    }
+    if (table[0] == 0) return set_error(MEMD_ERR_INVALID, "directions_noalloc: primes[0] must be nonzero");
+    for (int64_t c = 1; c < C; ++c)
+        if (table[c] < 2) return set_error(MEMD_ERR_INVALID, "directions_noalloc: bases must be >= 2");
+    int* d_table = nullptr;
+    memd_status st = noalloc_table(&d_table);
+    if (st != MEMD_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    // From pageable (stack) memory the copy has taken the data by the time it
+    // returns, so the table may go out of scope afterwards.  Every entry the
+    // kernel reads (0..C-1) is written here, so nothing needs clearing first.
+    cudaError_t e = cudaMemcpyAsync(d_table, table, sizeof(int) * (size_t)C, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return set_cuda_error("directions_noalloc: copy of the prime table", e);
+    k_directions<double><<<(unsigned)((K + 127) / 128), 128, 0, s>>>(d_table, (int)C, (int)K, d_dir);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error("directions_noalloc: launch", e);
+    return MEMD_OK;
+}
+
 }  // namespace memd
+
+extern "C" memd_status memd_directions_noalloc_f64(int64_t channels, int64_t directions, const int32_t* primes,
+                                                   double* d_dir, void* stream)
+{
+    return memd::directions_noalloc(channels, directions, primes, d_dir, stream);
+}
 
 extern "C" memd_status memd_directions_f64(int64_t channels, int64_t directions, const int32_t* primes,
                                            double* d_dir, void* stream)

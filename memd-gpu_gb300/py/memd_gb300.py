@@ -34,7 +34,7 @@ TRACE_DTYPE = np.dtype([("count", "<i4"), ("flags", "<i4"), ("hash", "<u8")])
 EXPORTS = [
     "memd_default_config", "memd_plan_create", "memd_plan_destroy", "memd_plan_workspace_bytes",
     "memd_plan_set_trace", "memd_run_f64", "memd_run_f32", "memd_run_batched_f64",
-    "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_directions_f64", "memd_directions_f32", "memd_diag_fma_rate", "memd_last_error",
+    "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64", "memd_diag_fma_rate", "memd_last_error",
     "memd_version", "memd_synth_tones", "memd_synth_eeg", "memd_write_bin", "memd_bin_count",
     "memd_read_bin",
 ]
@@ -121,7 +121,7 @@ def lib():
         f = getattr(L, name)
         f.argtypes = [vp, vp, vp, vp, vp, ctypes.POINTER(Profile)]
         f.restype = ctypes.c_int
-    for name in ("memd_directions_f64", "memd_directions_f32"):
+    for name in ("memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64"):
         f = getattr(L, name)
         f.argtypes = [i64, i64, vp, vp, vp]
         f.restype = ctypes.c_int

@@ -65,6 +65,43 @@ def _compile(src: str, extra_deps: list[str]) -> str:
     return obj
 
 
+EXAMPLES = ["sample_synthetic_signal", "memd_cli"]
+BINDIR = os.path.join(PKG, "bin")
+MEX_STUB_DIR = os.path.join(REPO, "tests", "mex_stub")
+MEX_STUB_LIB = os.path.join(LIBDIR, "libmemd_mex_stub.so")
+
+
+def _cuda_lib_dir() -> str:
+    for d in ("/usr/local/cuda/lib64", "/usr/local/cuda/targets/sbsa-linux/lib",
+              "/usr/local/cuda/targets/x86_64-linux/lib"):
+        if os.path.exists(os.path.join(d, "libcudart.so")):
+            return d
+    return "/usr/local/cuda/lib64"
+
+
+def _link_host(out: str, srcs: list[str], extra_inc: list[str], shared: bool) -> None:
+    deps = srcs + _headers() + [LIB]
+    if _newer(out, deps):
+        return
+    cmd = ["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", "-I/usr/local/cuda/include"]
+    cmd += [f"-I{d}" for d in extra_inc]
+    if shared:
+        cmd += ["-fPIC", "-shared"]
+    cmd += ["-o", out] + srcs + [f"-L{LIBDIR}", "-lmemd_gb300", f"-L{_cuda_lib_dir()}", "-lcudart",
+                                 f"-Wl,-rpath,{LIBDIR}", f"-Wl,-rpath,{_cuda_lib_dir()}"]
+    subprocess.check_call(cmd)
+
+
+def build_host_tools() -> None:
+    """The reference-style example driver, the .bin CLI and (for the tests)
+    the MEX entry linked against the stub of the mex/mxGPU API."""
+    os.makedirs(BINDIR, exist_ok=True)
+    for name in EXAMPLES:
+        _link_host(os.path.join(BINDIR, name), [os.path.join(PKG, "examples", name + ".cpp")], [], False)
+    _link_host(MEX_STUB_LIB, [os.path.join(PKG, "mex", "memd_mex.cpp"), os.path.join(MEX_STUB_DIR, "mex_stub.cpp")],
+               [MEX_STUB_DIR], True)
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
@@ -75,6 +112,7 @@ def build(verbose: bool = False) -> str:
     if not _newer(LIB, objs):
         cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         subprocess.check_call(cmd)
+    build_host_tools()
     if verbose:
         print("built", LIB)
     return LIB

@@ -21,10 +21,10 @@ size_t mxGetNumberOfElements(const mxArray* a);
 void mxFree(void* p);
 void mexErrMsgIdAndTxt(const char* id, const char* fmt, ...);
 int mexAtExit(void (*fn)(void));
+/* the MEX loader looks the gateway up by its unmangled name */
+void mexFunction(int nlhs, mxArray* plhs[], int nrhs, mxArray const* prhs[]);
 #ifdef __cplusplus
 }
 #endif
-
-void mexFunction(int nlhs, mxArray* plhs[], int nrhs, mxArray const* prhs[]);
 
 #endif

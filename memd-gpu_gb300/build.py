@@ -81,6 +81,9 @@ def _cuda_lib_dir() -> str:
 
 def _link_host(out: str, srcs: list[str], extra_inc: list[str], shared: bool) -> None:
     deps = srcs + _headers() + [LIB]
+    for d in extra_inc:
+        for root, _, files in os.walk(d):
+            deps += [os.path.join(root, f) for f in files if f.endswith(".h")]
     if _newer(out, deps):
         return
     cmd = ["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", "-I/usr/local/cuda/include"]

@@ -88,7 +88,13 @@ typedef struct {
     int32_t dir_chunk;     /* directions per pass (0 = all K at once) */
     int32_t solve_window;  /* tridiagonal halo in knots (0 = default; <0 = exact) */
     int32_t max_epochs;    /* batched runs: epochs per call (0 = single record) */
-    int64_t reserved[4];
+    int32_t mean_eval;     /* mean envelope: 0 = automatic (impulse accumulation
+                              for the mixed form in fixed mode, otherwise
+                              direct evaluation), 1 = direct evaluation of every
+                              envelope, 2 = impulse accumulation (mixed form,
+                              fixed mode only) */
+    int32_t reserved32;
+    int64_t reserved[3];
 } memd_config;
 
 typedef struct {

@@ -59,6 +59,8 @@ struct memd_plan {
     int GS, ngroups;
     int evalG, evalSPT, evalT;  // FP64 evaluation tile
     int ewG, ewSPL;             // FP32 / mixed evaluation tile
+    int cum, cumG;              // mixed fixed mode: impulse-accumulation mean, channels per lane group
+    int bpass;                  // (sift, chunk) passes enqueued so far in the decomposition being built
     size_t proj_smem, solve_smem;
     void* X;
     void* run;
@@ -69,6 +71,8 @@ struct memd_plan {
     void* sv;
     void* fac;
     void* rtab;
+    void* rtab3;  // impulse-accumulation mean: 1/(3h) as double-float
+    unsigned* bnd;  // impulse-accumulation mean: [2][C] per-channel bounds (float bits)
     void* M;     // stop mode: mean envelope of the last pass [L][C]
     void* part;  // stop mode: per channel group, direction and sample sum of (U-L)^2
     void* amp;   // stop mode: amplitude statistic [L]
@@ -163,6 +167,22 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
         MEMD_EVAL_CASES(MEMD_CASE)
 #undef MEMD_CASE
     } else {
+        if constexpr (P == MEMD_PREC_MIXED) {
+            if (p->cum) {
+                const unsigned* cur = p->bnd + (size_t)(p->bpass & 1) * g.C;
+                unsigned* other = p->bnd + (size_t)((p->bpass + 1) & 1) * g.C;
+#define MEMD_CASE(G_)                                                                                              \
+    if (p->cumG == G_) {                                                                                           \
+        dim3 grid((unsigned)g.W, (unsigned)((g.C + G_ - 1) / G_));                                                 \
+        k_mean_cum<G_><<<grid, 256, 0, s>>>((float2*)p->X, (dd*)p->acc, p->bits, p->wpref, p->knots, p->cnt,     \
+                                            (const dd*)p->rtab, (const dd*)p->rtab3, (const dd*)p->sv,           \
+                                            (const dd*)p->yv, cur, other, g, k0, kc, first, last, p->st);        \
+        return;                                                                                                    \
+    }
+                MEMD_CASE(32) MEMD_CASE(16) MEMD_CASE(8)
+#undef MEMD_CASE
+            }
+        }
         const bool stopm = p->cfg.stop_mode == MEMD_STOP_CRITERION;
 #define MEMD_CASE(G_, S_)                                                                                  \
     if (p->ewG == G_ && p->ewSPL == S_) {                                                                  \
@@ -255,11 +275,13 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         const long ns = 2L * kc * nseg * p->ngroups * p->GS;
         lc.begin();
         k_solve<R><<<(unsigned)((ns + kSolveThreads - 1) / kSolveThreads), kSolveThreads, p->solve_smem, s>>>(
-            (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->sv, g, k0, kc, p->S, p->H, p->GS, p->ngroups);
+            (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->sv, g, k0, kc, p->S, p->H, p->GS, p->ngroups,
+            p->cum ? p->bnd + (size_t)(p->bpass & 1) * g.C : nullptr);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
         lc.end(MEMD_STAGE_EVAL);
+        ++p->bpass;
         if (stop) {
             lc.begin();
             k_amp<R><<<(unsigned)((g.L + 255) / 256), 256, 0, s>>>((const R*)p->part, (R*)p->amp, p->cnt, g, k0, kc,
@@ -293,6 +315,8 @@ static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
     const int nimf = (int)p->cfg.num_imfs;
     const int maxit = (int)p->cfg.max_iter;
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
+    p->bpass = 0;
+    if (p->cum) cudaMemsetAsync(p->bnd, 0, sizeof(unsigned) * 2 * (size_t)g.C, s);
     for (int i = 0; i + 1 < nimf; ++i) {
         cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, s);
         for (int j = 0; j < maxit; ++j) {
@@ -671,6 +695,19 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         p->ewSPL = 32;
     }
     p->egroups = (C + (f64 ? p->evalG : p->ewG) - 1) / (f64 ? p->evalG : p->ewG);
+    // mean envelope: impulse accumulation for the mixed form in fixed mode
+    // (mean_eval 0 = automatic, 1 = direct evaluation, 2 = impulse accumulation)
+    if (c.mean_eval < 0 || c.mean_eval > 2) {
+        delete p;
+        return set_error(MEMD_ERR_INVALID, "plan: mean_eval must be 0, 1 or 2");
+    }
+    const bool cum_ok = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED;
+    if (c.mean_eval == 2 && !cum_ok) {
+        delete p;
+        return set_error(MEMD_ERR_UNSUPPORTED, "plan: impulse-accumulation mean needs the mixed form in fixed mode");
+    }
+    p->cum = cum_ok && c.mean_eval != 1;
+    p->cumG = C >= 32 ? 32 : (C > 8 ? 16 : 8);
     const size_t rb = (size_t)p->real_bytes;
     if (c.precision == MEMD_PREC_MIXED)
         p->proj_smem = 4 * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2) + C + kProjTK);
@@ -697,6 +734,10 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->rtab, rb * (size_t)(L + 1));
+    if (p->cum) {
+        ALLOC(p->rtab3, sizeof(dd) * (size_t)(L + 1));
+        ALLOC(p->bnd, sizeof(unsigned) * 2 * (size_t)C);
+    }
     if (c.stop_mode == MEMD_STOP_CRITERION) {
         ALLOC(p->M, rb * CL);
         ALLOC(p->part, rb * (size_t)p->egroups * Kc * L);
@@ -727,7 +768,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         if (e == cudaSuccess) e = cudaMalloc((void**)&r32, sizeof(float) * (size_t)(L + 1));
         if (e == cudaSuccess) e = cudaMalloc((void**)&rdd, sizeof(dd) * (size_t)(L + 1));
         if (e == cudaSuccess) {
-            k_fill_reciprocals<<<256, 256>>>(r64, r32, rdd, L + 1);
+            k_fill_reciprocals<<<256, 256>>>(r64, r32, rdd, (dd*)p->rtab3, L + 1);
             const void* src = f64 ? (void*)r64 : (c.precision == MEMD_PREC_MIXED ? (void*)rdd : (void*)r32);
             e = cudaMemcpy(p->rtab, src, rb * (size_t)(L + 1), cudaMemcpyDeviceToDevice);
         }

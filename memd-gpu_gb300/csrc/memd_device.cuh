@@ -214,5 +214,9 @@ __device__ __forceinline__ dd sqrt_(dd a) { return dd_sqrt(a); }
 __device__ __forceinline__ double fmat_(double a, float t, double c) { return __fma_rn(a, (double)t, c); }
 __device__ __forceinline__ float fmat_(float a, float t, float c) { return __fmaf_rn(a, t, c); }
 __device__ __forceinline__ dd fmat_(dd a, float t, dd c) { return dd_mulf(a, t) + c; }
+// magnitude as a float (bounds only: the float may round down by 1 ulp)
+__device__ __forceinline__ float magf(double v) { return (float)fabs(v); }
+__device__ __forceinline__ float magf(float v) { return fabsf(v); }
+__device__ __forceinline__ float magf(dd v) { return fabsf(v.hi); }
 
 }  // namespace memd

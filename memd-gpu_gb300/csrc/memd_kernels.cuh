@@ -302,8 +302,12 @@ constexpr int kSolveThreads = 128;
 template <typename real>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
-        real* __restrict__ sv, Geom g, int k0, int Kc, int S, int H, int GS, int ngroups)
+        real* __restrict__ sv, Geom g, int k0, int Kc, int S, int H, int GS, int ngroups,
+        unsigned* __restrict__ bnd)
 {
+    // bnd != nullptr: also raise bnd[c] (float bits) to a bound on |S(n)| over
+    // this segment's pieces: max|y| + h^2 (|s_i| + |s_{i+1}|) / 4 (the linear
+    // interpolant plus h^2/8 max|S''|), used by the impulse-accumulation mean.
     extern __shared__ __align__(16) unsigned char smem_raw[];
     real* halo = reinterpret_cast<real*>(smem_raw);  // [max(H,0)][kSolveThreads]
     const long gl = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -336,9 +340,11 @@ k_solve(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real
     if (is > 0) slope_prev = mul_(sub_(yi, y[(size_t)(is - 1) * C]), f[is - 1].ih);
     real dprev = real(0);
     real ynext = (is < E - 1) ? y[(size_t)(is + 1) * C] : real(0);
+    float ymax = 0.0f;
 #pragma unroll 4
     for (int i = is; i < ie; ++i) {
         const Fac<real> fi = f[i];
+        if (i >= i0 && i <= i1) ymax = fmaxf(ymax, magf(yi));
         const real yafter = (i + 2 < E) ? y[(size_t)(i + 2) * C] : real(0);
         real slope = real(0), r = real(0);
         if (i < E - 1) slope = mul_(sub_(ynext, yi), fi.ih);
@@ -354,13 +360,21 @@ k_solve(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real
         dprev = dcur;
     }
     real snext = real(0);
+    float spart = 0.0f;
 #pragma unroll 4
     for (int i = ie - 1; i >= i0; --i) {
         const real d = (i >= i1) ? halo[(i - i1) * kSolveThreads + threadIdx.x] : o[(size_t)i * C];
         const real sol = fmad_(-f[i].cp, snext, d);
-        if (i < i1) o[(size_t)i * C] = sol;
+        if (i < i1) {
+            o[(size_t)i * C] = sol;
+            if (bnd && i < E - 1) {
+                const float ih = magf(f[i].ih);
+                spart = fmaxf(spart, __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih));
+            }
+        }
         snext = sol;
     }
+    if (bnd) atomicMax(&bnd[c], __float_as_uint((ymax + spart) * 1.01f));
 }
 
 // ---------------------------------------------------------------------------
@@ -757,6 +771,192 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// Mean envelope by impulse accumulation (mixed form, fixed mode).
+//
+// A natural cubic spline with knots x_j is, for n >= x_0,
+//     S(n) = P_0(n) + sum_j dd_j (n - x_j)_+^3,   dd_j = d_j - d_{j-1}
+// (the pieces agree in value, slope and curvature at every interior knot;
+// only the cubic coefficient d jumps).  The fourth forward difference of
+// (n - x)_+^3 is 1, 4, 1 at n = x-3, x-2, x-1 and zero elsewhere, so the sum
+// over all envelopes M(n) = sum_e S_e(n) obeys
+//     Delta^4 M(n) = I(n) = sum over interior knots of dd_j * {1,4,1}.
+// Per 32-sample word the kernel anchors M at the middle sample n_a (value and
+// the first three forward differences of the pieces active there, plus the
+// impulses that knots at n_a+1, n_a+2 place before n_a), then rebuilds M(n)
+// by running the difference recurrence forwards and backwards over the word.
+// Work per word: O(knots + envelopes) instead of O(envelopes x samples).
+//
+// All anchors, impulses and the recurrence are integers in units of
+// q = 2^(e - 62), 2^e > 2 Kc B_c, with B_c a bound on |S_e(n)| for channel c
+// written by the solve (max |y| + h^2 (|s_i| + |s_{i+1}|) / 4 over the pieces):
+// the sums are exact and independent of the order of the directions.  The
+// double-float inputs carry ~48 bits, and the recurrence extrapolates each
+// anchor over at most 16 samples, which keeps the mean within ~1e-13 of its
+// value relative to the signal (the direct evaluation: ~1e-15).
+//
+// CTA: one word x G channels, 8 warps; lane = (subgroup, channel), the
+// (direction, envelope) pairs are dealt round-robin to the 8 * 32/G
+// subgroups, whose impulses meet in shared memory (64-bit integer atomics).
+// Warp 0 then runs the forward half of the recurrence, warp 1 the backward.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long qfix(dd v, float sc)
+{
+    return (unsigned long long)__float2ll_rn(__fmul_rn(v.hi, sc)) +
+           (unsigned long long)__float2ll_rn(__fmul_rn(v.lo, sc));
+}
+
+template <int G>
+__global__ void __launch_bounds__(256)
+k_mean_cum(float2* __restrict__ X, dd* __restrict__ acc_buf, const uint32_t* __restrict__ bits,
+           const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
+           const dd* __restrict__ rtab, const dd* __restrict__ rtab3, const dd* __restrict__ sv,
+           const dd* __restrict__ yv, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear, Geom g,
+           int k0, int Kc, int first_chunk, int last_chunk, RunState* st)
+{
+    constexpr int SUB = 32 / G;
+    constexpr int NWS = 8 * SUB;
+    __shared__ unsigned long long imp[32 * G];
+    __shared__ unsigned long long anc[6 * G];
+    __shared__ int sQ;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cc = lane % G, sub = lane / G;
+    const int w = blockIdx.x;
+    const int p0 = w * 32;
+    const int nl = min(32, g.L - p0);
+    const int ra = min(16, nl - 1);
+    const int na = p0 + ra;
+    const int C = g.C;
+    const int c = blockIdx.y * G + cc;
+    const bool cok = c < C;
+    const int cl = min(c, C - 1);  // loads of lanes past the last channel stay in bounds
+    for (int i = threadIdx.x; i < 32 * G; i += blockDim.x) imp[i] = 0ull;
+    for (int i = threadIdx.x; i < 6 * G; i += blockDim.x) anc[i] = 0ull;
+    if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)
+        for (int i = threadIdx.x; i < C; i += blockDim.x) bnd_clear[i] = 0u;
+    if (warp == 0) {
+        int q = 0;
+        for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        q = warp_sum(q);
+        if (lane == 0) sQ = q;
+    }
+    // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex
+    const float B = __uint_as_float(bnd[cl]);
+    const bool bad = !(B < INFINITY);
+    int ex = 0;
+    frexpf(__fmul_rn(B, (float)(2 * Kc)) * 1.0009765625f, &ex);
+    ex = max(ex, -60);
+    const float sc = ldexpf(1.0f, 62 - ex);  // value -> units
+    const float qv = ldexpf(1.0f, ex - 62);  // units -> value
+    const dd third = dd(1.0 / 3.0);
+    __syncthreads();
+
+    unsigned long long aA = 0, aB = 0, aC = 0, aD = 0, la2 = 0, la3 = 0;
+    const int xend = p0 + nl + 2;  // knots up to here place impulses in the word
+    for (int ei = warp * SUB + sub; ei < 2 * Kc; ei += NWS) {
+        const int kk = ei >> 1, env = ei & 1;
+        const int k = k0 + kk;
+        const int Ex = cnt[k], En = cnt[g.K + k];
+        if (!(Ex > 3 && En > 3) || Ex > g.cap || En > g.cap) continue;
+        const int E = env ? En : Ex;
+        const size_t slot = (size_t)env * Kc + kk;
+        const uint32_t bw = bits[slot * g.W + w];
+        const int wp = wpref[slot * (g.W + 1) + w];
+        const int* kn = knots + slot * g.cap;
+        const dd* sc_ = sv + slot * (size_t)g.cap * C + cl;
+        const dd* yc_ = yv + slot * (size_t)g.cap * C + cl;
+        // anchor: the piece [x_i, x_{i+1}] with x_i <= n_a < x_{i+1}
+        {
+            const uint32_t le = (ra == 31) ? bw : (bw & ((2u << ra) - 1u));
+            const int i = min(wp + __popc(le) - 1, E - 2);
+            const int xi = kn[i], h = kn[i + 1] - xi;
+            const dd y0 = yc_[(size_t)i * C], y1 = yc_[(size_t)(i + 1) * C];
+            const dd s0 = sc_[(size_t)i * C], s1 = sc_[(size_t)(i + 1) * C];
+            const dd d = (s1 - s0) * rtab3[h];
+            const dd b = (y1 - y0) * rtab[h] - dd_mulf(dd_mulf(s0, 2.0f) + s1, (float)h) * third;
+            const float u = (float)(na - xi);
+            const dd d3 = dd_mulf(d, 3.0f);
+            aA += qfix(dd_mulf(dd_mulf(dd_mulf(d, u) + s0, u) + b, u) + y0, sc);
+            aB += qfix(dd_mulf(dd_mulf(d3, u) + dd_mulf(s0, 2.0f), u) + b, sc);
+            aC += qfix(dd_mulf(d3, u) + s0, sc);
+            aD += qfix(d, sc);
+        }
+        // impulses of the interior knots x_j in (p0, p0 + nl + 2]
+        int j = max(1, wp + (int)(bw & 1u));
+        if (j <= E - 2) {
+            int xj = kn[j];
+            if (xj <= xend) {
+                const int xp = kn[j - 1];
+                dd scur = sc_[(size_t)j * C];
+                dd dprev = (scur - sc_[(size_t)(j - 1) * C]) * rtab3[xj - xp];
+                for (;;) {
+                    const int xn = kn[j + 1];
+                    const dd sn = sc_[(size_t)(j + 1) * C];
+                    const dd dcur = (sn - scur) * rtab3[xn - xj];
+                    const unsigned long long qd = qfix(dcur - dprev, sc);
+                    const int r = xj - 3 - p0;
+                    if (r >= 0 && r < nl) atomicAdd(&imp[r * G + cc], qd);
+                    if (r + 1 >= 0 && r + 1 < nl) atomicAdd(&imp[(r + 1) * G + cc], qd << 2);
+                    if (r + 2 >= 0 && r + 2 < nl) atomicAdd(&imp[(r + 2) * G + cc], qd);
+                    if (xj == na + 1) {
+                        la2 += qd;
+                        la3 += 5ull * qd;
+                    } else if (xj == na + 2) {
+                        la3 += qd;
+                    }
+                    ++j;
+                    if (j > E - 2 || xn > xend) break;
+                    xj = xn;
+                    scur = sn;
+                    dprev = dcur;
+                }
+            }
+        }
+    }
+    atomicAdd(&anc[0 * G + cc], aA);
+    atomicAdd(&anc[1 * G + cc], aB);
+    atomicAdd(&anc[2 * G + cc], aC);
+    atomicAdd(&anc[3 * G + cc], aD);
+    atomicAdd(&anc[4 * G + cc], la2);
+    atomicAdd(&anc[5 * G + cc], la3);
+    __syncthreads();
+    const int Q = sQ;
+    if (last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
+    if (warp >= 2 || sub != 0 || !cok) return;
+    const unsigned long long sA = anc[cc], sB = anc[G + cc], sC = anc[2 * G + cc], sD = anc[3 * G + cc];
+    unsigned long long v = sA, d1 = sB + sC + sD, d2 = 2ull * sC + 6ull * sD + anc[4 * G + cc],
+                       d3 = 6ull * sD + anc[5 * G + cc];
+    const dd qd = dd((float)Q, 0.0f);
+    auto emit = [&](int r, unsigned long long val) {
+        const long long vi = (long long)val;
+        const float hi = __ll2float_rn(vi);
+        const float lo = __ll2float_rn(vi - __float2ll_rn(hi));
+        dd tot(__fmul_rn(hi, qv), __fmul_rn(lo, qv));
+        if (bad) tot = dd(__int_as_float(0x7fc00000), 0.0f);
+        const size_t off = (size_t)(p0 + r) * C + c;
+        if (!first_chunk) tot = tot + acc_buf[off];
+        if (last_chunk) X[off] = xsub(X[off], dd_mulf(tot, 0.5f) / qd);
+        else acc_buf[off] = tot;
+    };
+    if (warp == 0) {
+        for (int r = ra; r < nl; ++r) {
+            emit(r, v);
+            v += d1;
+            d1 += d2;
+            d2 += d3;
+            d3 += imp[r * G + cc];
+        }
+    } else {
+        for (int r = ra - 1; r >= 0; --r) {
+            d3 -= imp[r * G + cc];
+            d2 -= d3;
+            d1 -= d2;
+            v -= d1;
+            emit(r, v);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Projection + extrema for the mixed path: P = dir . X in FP32 from the high
 // words of the double-float signal, with a rigorous bound on its error
 //   |P32 - P| <= (C+2) 2^-24 sum_c |dh_c| max|xh_c| + sum_c |dl_c| max|X_c|
@@ -1123,13 +1323,16 @@ __global__ void k_check_coords(const int32_t* __restrict__ x, int L, int* __rest
         if (x[n] != n) atomicOr(bad, 1);
 }
 
-__global__ void k_fill_reciprocals(double* __restrict__ r64, float* __restrict__ r32, dd* __restrict__ rdd, int n)
+__global__ void k_fill_reciprocals(double* __restrict__ r64, float* __restrict__ r32, dd* __restrict__ rdd,
+                                   dd* __restrict__ r3dd, int n)
 {
+    // r3dd (optional): 1/(3h) as a double-float
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < n; h += gridDim.x * blockDim.x) {
         const double r = h > 0 ? __ddiv_rn(1.0, (double)h) : 0.0;
         r64[h] = r;
         r32[h] = h > 0 ? __fdiv_rn(1.0f, (float)h) : 0.0f;
         rdd[h] = dd(r);
+        if (r3dd) r3dd[h] = h > 0 ? dd(__ddiv_rn(1.0, 3.0 * (double)h)) : dd(0.0f, 0.0f);
     }
 }
 

@@ -62,7 +62,9 @@ class Config(ctypes.Structure):
         ("dir_chunk", ctypes.c_int32),
         ("solve_window", ctypes.c_int32),
         ("max_epochs", ctypes.c_int32),
-        ("reserved", ctypes.c_int64 * 4),
+        ("mean_eval", ctypes.c_int32),
+        ("reserved32", ctypes.c_int32),
+        ("reserved", ctypes.c_int64 * 3),
     ]
 
 

@@ -44,11 +44,23 @@ def test_version_and_default_config(lib):
     dict(channels=2, length=100, directions=4, num_imfs=0),
     dict(channels=2, length=100, directions=4, max_iter=-1),
     dict(channels=2, length=100, directions=4, precision=7),
+    dict(channels=2, length=100, directions=4, mean_eval=3),
 ])
 def test_plan_rejects_bad_config_on_host(kw):
     with pytest.raises(memd_gb300.MemdError) as ei:
         memd_gb300.Plan(**kw)
     assert ei.value.status == memd_gb300.MEMD_ERR_INVALID
+
+
+@pytest.mark.parametrize("kw", [
+    dict(precision=memd_gb300.PREC_F64, mean_eval=2),
+    dict(precision=memd_gb300.PREC_F32, mean_eval=2),
+    dict(precision=memd_gb300.PREC_MIXED, mean_eval=2, stop_mode=memd_gb300.STOP_CRITERION),
+])
+def test_impulse_mean_only_for_mixed_fixed_mode(kw):
+    with pytest.raises(memd_gb300.MemdError) as ei:
+        memd_gb300.Plan(2, 100, 4, **kw)
+    assert ei.value.status == memd_gb300.MEMD_ERR_UNSUPPORTED
 
 
 def test_null_plan_arguments(lib):

@@ -250,3 +250,33 @@ def test_mixed_stop_mode_runs():
     b, sb, _ = run_gpu(y32, d32, 10, 50, precision=mg.PREC_MIXED, stop_mode=mg.STOP_CRITERION)
     assert sb.n_imfs >= 1
     assert np.abs(b.astype(np.float64).sum(axis=0) - y32).max() < 1e-4 * np.abs(y32).max()
+
+
+@pytest.mark.parametrize("C,L,K,chunk", [(8, 2000, 64, 0), (5, 3000, 16, 0), (40, 4000, 24, 0),
+                                         (32, 8192, 64, 0), (12, 5000, 40, 16)])
+def test_mixed_impulse_mean_matches_fp64_sets(C, L, K, chunk):
+    """Mixed form, fixed mode: the impulse-accumulation mean (default) and the
+    direct evaluation of every envelope give the FP64 path's extrema sets at
+    every sift; IMFs agree with FP64 to the float32 output rounding."""
+    y = eeg(C, L, seed=31) if C > 8 else mg.synth_tones(C, L, 1000.0, seed=5)
+    d = oracle.directions(C, K)
+    y32, d32, y64, d64 = _as_f32_inputs(y, d)
+    nimf = 6
+    a, sa, ta = run_gpu(y64, d64, nimf, 10, trace=True)
+    b, sb, tb = run_gpu(y32, d32, nimf, 10, precision=mg.PREC_MIXED, trace=True, dir_chunk=chunk)
+    c, sc, tc = run_gpu(y32, d32, nimf, 10, precision=mg.PREC_MIXED, trace=True, dir_chunk=chunk, mean_eval=1)
+    for t in (tb, tc):
+        assert np.array_equal(ta["count"][: nimf - 1, :10], t["count"][: nimf - 1, :10])
+        assert np.array_equal(ta["hash"][: nimf - 1, :10], t["hash"][: nimf - 1, :10])
+    for i in range(nimf):
+        assert rel_l2(b[i], a[i]) < 1e-6, i
+        assert rel_l2(b[i], c[i]) < 1e-6, i
+    assert sb.flags == 0 and sc.flags == 0
+
+
+def test_mixed_impulse_mean_nan_when_no_direction_qualifies():
+    y = np.tile(np.arange(96, dtype=np.float32), (4, 1))  # monotone: no interior extrema
+    d = oracle.directions(4, 8).astype(np.float32)
+    b, sb, _ = run_gpu(y, d, 2, 1, precision=mg.PREC_MIXED)
+    assert sb.flags & mg.FLAG_NO_QUALIFIED_DIRECTION
+    assert np.isnan(b[0]).all()

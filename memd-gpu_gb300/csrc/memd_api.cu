@@ -55,13 +55,13 @@ struct memd_plan {
     int xbytes;      // working-signal storage
     int tbytes;      // caller's element type
     int Kc, nchunks;
-    int S, H, Sf, Hf;
+    int S, H, Sf, Hf, Ss;  // solve segments (long / short systems) and halo; factor segments and halo
     int GS, ngroups;
     int evalG, evalSPT, evalT;  // FP64 evaluation tile
     int ewG, ewSPL;             // FP32 / mixed evaluation tile
     int cum, cumG;              // mixed fixed mode: impulse-accumulation mean, channels per lane group
     int bpass;                  // (sift, chunk) passes enqueued so far in the decomposition being built
-    size_t proj_smem, solve_smem;
+    size_t proj_smem;
     void* X;
     void* run;
     void* dir;   // FP64/FP32: K x C; mixed: high words then low words
@@ -69,10 +69,11 @@ struct memd_plan {
     void* imf;
     void* yv;
     void* sv;
+    void* dbuf;  // forward-eliminated right-hand sides [2][Kc][cap][C]
     void* fac;
     void* rtab;
     void* rtab3;  // impulse-accumulation mean: 1/(3h) as double-float
-    unsigned* bnd;  // impulse-accumulation mean: [2][C] per-channel bounds (float bits)
+    unsigned* bnd;  // impulse-accumulation mean: [2 passes][2 parts][C] per-channel bounds (float bits)
     void* M;     // stop mode: mean envelope of the last pass [L][C]
     void* part;  // stop mode: per channel group, direction and sample sum of (U-L)^2
     void* amp;   // stop mode: amplitude statistic [L]
@@ -169,8 +170,8 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
     } else {
         if constexpr (P == MEMD_PREC_MIXED) {
             if (p->cum) {
-                const unsigned* cur = p->bnd + (size_t)(p->bpass & 1) * g.C;
-                unsigned* other = p->bnd + (size_t)((p->bpass + 1) & 1) * g.C;
+                const unsigned* cur = p->bnd + (size_t)(p->bpass & 1) * 2 * g.C;
+                unsigned* other = p->bnd + (size_t)((p->bpass + 1) & 1) * 2 * g.C;
 #define MEMD_CASE(G_)                                                                                              \
     if (p->cumG == G_) {                                                                                           \
         dim3 grid((unsigned)g.W, (unsigned)((g.C + G_ - 1) / G_));                                                 \
@@ -235,8 +236,6 @@ static cudaError_t set_attrs(memd_plan* p)
     else
         e = cudaFuncSetAttribute(k_project_extrema<R, XT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)p->proj_smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_solve<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(p->solve_smem, 1));
     return e;
 }
 
@@ -271,12 +270,17 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         k_factor<R><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
                                                                  (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf);
         lc.end(MEMD_STAGE_FACTOR);
-        const long nseg = (g.cap + p->S - 1) / p->S;
-        const long ns = 2L * kc * nseg * p->ngroups * p->GS;
+        const long nseg = (p->H < 0) ? 1 : (g.cap + p->Ss - 1) / p->Ss;
+        const long ns = 2L * kc * nseg * p->ngroups * 32;
+        const unsigned nb = (unsigned)((ns + kSolveThreads - 1) / kSolveThreads);
+        unsigned* bcur = p->cum ? p->bnd + (size_t)(p->bpass & 1) * 2 * g.C : nullptr;
         lc.begin();
-        k_solve<R><<<(unsigned)((ns + kSolveThreads - 1) / kSolveThreads), kSolveThreads, p->solve_smem, s>>>(
-            (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->sv, g, k0, kc, p->S, p->H, p->GS, p->ngroups,
-            p->cum ? p->bnd + (size_t)(p->bpass & 1) * g.C : nullptr);
+        k_solve_fwd<R><<<nb, kSolveThreads, 0, s>>>((const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0,
+                                                   kc, p->S, p->Ss, p->H, p->ngroups, bcur);
+        lc.end(MEMD_STAGE_SOLVE);
+        lc.begin();
+        k_solve_bwd<R><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0,
+                                                   kc, p->S, p->Ss, p->H, p->ngroups, bcur);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
@@ -316,7 +320,7 @@ static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
     const int maxit = (int)p->cfg.max_iter;
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
     p->bpass = 0;
-    if (p->cum) cudaMemsetAsync(p->bnd, 0, sizeof(unsigned) * 2 * (size_t)g.C, s);
+    if (p->cum) cudaMemsetAsync(p->bnd, 0, sizeof(unsigned) * 4 * (size_t)g.C, s);
     for (int i = 0; i + 1 < nimf; ++i) {
         cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, s);
         for (int j = 0; j < maxit; ++j) {
@@ -654,6 +658,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     p->nchunks = (K + p->Kc - 1) / p->Kc;
     if (c.solve_window < 0) {
         p->S = p->g.cap;
+        p->Ss = p->g.cap;
         p->H = -1;
         p->Sf = p->g.cap;
         p->Hf = -1;
@@ -662,12 +667,13 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         // <= 1/3 (pivots) per knot; FP64 and double-float need ~1e-15
         const bool wide = f64 || c.precision == MEMD_PREC_MIXED;
         p->S = 256;
+        p->Ss = 64;
         p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : (wide ? 32 : 24));
         p->Sf = 64;
         p->Hf = wide ? 40 : 20;
     }
-    p->GS = std::min(32, next_pow2(C));
-    p->ngroups = (C + p->GS - 1) / p->GS;
+    p->GS = 32;  // solve: one warp per (envelope, direction, segment, 32 channels)
+    p->ngroups = (C + 31) / 32;
     // FP64 evaluation tile: G channels x T samples, enough CTAs to fill the GPU
     p->evalG = std::min(32, std::max(4, next_pow2(C)));
     {
@@ -713,7 +719,6 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         p->proj_smem = 4 * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2) + C + kProjTK);
     else
         p->proj_smem = rb * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2));
-    p->solve_smem = p->H > 0 ? rb * (size_t)p->H * kSolveThreads : 0;
     const size_t CL = (size_t)C * L;
     const size_t Kc = (size_t)p->Kc;
     memd_status st = MEMD_OK;
@@ -733,10 +738,11 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
     ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
+    ALLOC(p->dbuf, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->rtab, rb * (size_t)(L + 1));
     if (p->cum) {
         ALLOC(p->rtab3, sizeof(dd) * (size_t)(L + 1));
-        ALLOC(p->bnd, sizeof(unsigned) * 2 * (size_t)C);
+        ALLOC(p->bnd, sizeof(unsigned) * 4 * (size_t)C);
     }
     if (c.stop_mode == MEMD_STOP_CRITERION) {
         ALLOC(p->M, rb * CL);

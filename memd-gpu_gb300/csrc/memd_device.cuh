@@ -203,6 +203,12 @@ __device__ __forceinline__ dd sub_(dd a, dd b) { return a - b; }
 __device__ __forceinline__ dd div_(dd a, dd b) { return a / b; }
 __device__ __forceinline__ double shfl_xor_(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 __device__ __forceinline__ float shfl_xor_(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_idx_(double v, int l) { return __shfl_sync(0xffffffffu, v, l); }
+__device__ __forceinline__ float shfl_idx_(float v, int l) { return __shfl_sync(0xffffffffu, v, l); }
+__device__ __forceinline__ dd shfl_idx_(dd v, int l)
+{
+    return dd(__shfl_sync(0xffffffffu, v.hi, l), __shfl_sync(0xffffffffu, v.lo, l));
+}
 __device__ __forceinline__ dd shfl_xor_(dd v, int o)
 {
     return dd(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));

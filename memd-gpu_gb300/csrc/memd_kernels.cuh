@@ -13,8 +13,10 @@
 //   k_factor           channel-independent Thomas factorisation of the
 //                      natural-spline system (REF:704-736; replaces the
 //                      factorisation inside cusparse gtsv2_nopivot)
-//   k_solve            forward/backward substitution for every channel, in
-//                      windows of S knots with an H-knot halo (REF:1227-1241)
+//   k_solve_fwd/bwd    forward and backward substitution for every channel,
+//                      in windows of S knots with an H-knot halo (REF:1227-1241)
+//   k_mean_cum         mixed form, fixed mode: the mean envelope rebuilt from
+//                      per-knot impulses and per-word anchors (REF:775-864)
 //   k_eval             spline coefficients per interval, envelope evaluation
 //                      fused with the mean over directions and the update of
 //                      the working signal (REF:775-864)
@@ -288,93 +290,171 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
 }
 
 // ---------------------------------------------------------------------------
-// Substitution.  A group of GS lanes (GS | 32) handles one (envelope,
-// direction, segment, channel group); each lane one channel.  The forward
-// sweep runs over [i0-H, i1+H), the backward sweep from i1+H-1 down to i0;
-// both recurrences contract (multipliers <= 2/3 and <= 1/2 per row), so the
-// window's truncated starts perturb the segment by at most that factor to the
-// power H.  H < 0 selects the exact single-window solve.
-// The halo values of the forward sweep live in shared memory, the segment's
-// own values go straight to sy and are overwritten by the solution.
+// Substitution, as two kernels.  A warp handles one (envelope, direction,
+// segment, group of 32 channels); each lane one channel (lanes past the last
+// channel compute on a copy of it and store nothing).
+//   k_solve_fwd: forward sweep over [i0-H, i1), writing the eliminated right
+//                -hand side d of rows [i0, i1) to dbuf;
+//   k_solve_bwd: backward sweep from i1+H-1 down to i0, reading d of the
+//                segment and of the next segment's first H rows from dbuf,
+//                writing the solution of rows [i0, i1) to sv.
+// Rows go in batches of 16: every lane loads its 16 values at once, lanes
+// 0..15 load the batch's factor rows, which the sweep takes by shuffle, so a
+// batch costs one memory round trip instead of one per row.
+// Both recurrences contract (multipliers <= 2/3 and <= 1/2 per row), so a
+// window's truncated start perturbs the segment by at most that factor to the
+// power H; the rows a thread reads from the next segment are that segment's
+// own converged values, so the result does not depend on the segmentation.
+// H < 0 selects the exact single-window solve.  Segments hold S knots when
+// the system has more than 16 S knots, otherwise Ss (more, shorter segments
+// keep the GPU busy when the knot sets are short).  The segment index is the
+// slowest grid index, so whole CTAs past the active segments exit at once.
+// bnd != nullptr: raise bnd[c] (forward: max |y| over the segment's knots) and
+// bnd[C + c] (backward: max h^2 (|s_i| + |s_{i+1}|) / 4 over its pieces), float
+// bits; their sum bounds |S(n)| (the linear interpolant plus h^2/8 max|S''|).
 // ---------------------------------------------------------------------------
 constexpr int kSolveThreads = 128;
+constexpr int kSolveBatch = 16;
+
+struct SolveItem {
+    int env, kk, seg, c, i0, i1, E;
+    bool ok;
+};
+
+__device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, int k0, int Kc, int S, int Ss, int H,
+                                                int ngroups)
+{
+    SolveItem it;
+    const long gw = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp = item
+    const int cgi = (int)(gw % ngroups);
+    const long item = gw / ngroups;
+    const int slot = (int)(item % (2 * Kc));
+    it.seg = (int)(item / (2 * Kc));
+    it.env = slot / Kc;
+    it.kk = slot - it.env * Kc;
+    it.c = cgi * 32 + (int)(threadIdx.x & 31);
+    it.ok = false;
+    it.E = cnt[it.env * g.K + k0 + it.kk];
+    if (it.E > g.cap || it.E < 2) return it;
+    const int Se = (H < 0) ? g.cap : (it.E > 16 * S ? S : Ss);
+    it.i0 = it.seg * Se;
+    if (it.i0 >= it.E) return it;
+    it.i1 = min(it.E, it.i0 + Se);
+    it.ok = true;
+    return it;
+}
 
 template <typename real>
 __global__ void __launch_bounds__(kSolveThreads)
-k_solve(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
-        real* __restrict__ sv, Geom g, int k0, int Kc, int S, int H, int GS, int ngroups,
-        unsigned* __restrict__ bnd)
+k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
+            real* __restrict__ dbuf, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
+            unsigned* __restrict__ bnd)
 {
-    // bnd != nullptr: also raise bnd[c] (float bits) to a bound on |S(n)| over
-    // this segment's pieces: max|y| + h^2 (|s_i| + |s_{i+1}|) / 4 (the linear
-    // interpolant plus h^2/8 max|S''|), used by the impulse-accumulation mean.
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    real* halo = reinterpret_cast<real*>(smem_raw);  // [max(H,0)][kSolveThreads]
-    const long gl = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = (int)(gl % GS);
-    long item = gl / GS;
-    const int nseg = (g.cap + S - 1) / S;
-    const int cgi = (int)(item % ngroups);
-    item /= ngroups;
-    const int seg = (int)(item % nseg);
-    item /= nseg;
-    const int kk = (int)(item % Kc);
-    const int env = (int)(item / Kc);
-    if (env >= 2) return;
-    const int E = cnt[env * g.K + k0 + kk];
-    if (E > g.cap || E < 2) return;
-    const int i0 = seg * S;
-    if (i0 >= E) return;
-    const int i1 = min(E, i0 + S);
-    const int c = cgi * GS + lane;
-    if (c >= g.C) return;
-    const int C = g.C;
-    const size_t slot = (size_t)env * Kc + kk;
+    constexpr int B = kSolveBatch;
+    const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
+    if (!it.ok) return;  // uniform over the warp
+    const int lane = threadIdx.x & 31;
+    const int C = g.C, E = it.E, i0 = it.i0, i1 = it.i1;
+    const bool cok = it.c < C;
+    const int cl = min(it.c, C - 1);
+    const size_t slot = (size_t)it.env * Kc + it.kk;
     const Fac<real>* f = fac + slot * g.cap;
-    const real* y = yv + slot * (size_t)g.cap * C + c;
-    real* o = sv + slot * (size_t)g.cap * C + c;
+    const real* y = yv + slot * (size_t)g.cap * C + cl;
+    real* o = dbuf + slot * (size_t)g.cap * C + cl;
     const int is = (H < 0) ? 0 : max(0, i0 - H);
-    const int ie = (H < 0) ? E : min(E, i1 + H);
     real yi = y[(size_t)is * C];
     real slope_prev = real(0);
     if (is > 0) slope_prev = mul_(sub_(yi, y[(size_t)(is - 1) * C]), f[is - 1].ih);
     real dprev = real(0);
-    real ynext = (is < E - 1) ? y[(size_t)(is + 1) * C] : real(0);
     float ymax = 0.0f;
-#pragma unroll 4
-    for (int i = is; i < ie; ++i) {
-        const Fac<real> fi = f[i];
-        if (i >= i0 && i <= i1) ymax = fmaxf(ymax, magf(yi));
-        const real yafter = (i + 2 < E) ? y[(size_t)(i + 2) * C] : real(0);
-        real slope = real(0), r = real(0);
-        if (i < E - 1) slope = mul_(sub_(ynext, yi), fi.ih);
-        if (i > 0 && i < E - 1) r = mul_(real(3), sub_(slope, slope_prev));
-        const real dcur = fmad_(-fi.lm, dprev, mul_(fi.m, r));
-        // rows before i0 only warm the recurrence up: they belong to the
-        // previous segment, which writes them itself
-        if (i >= i1) halo[(i - i1) * kSolveThreads + threadIdx.x] = dcur;
-        else if (i >= i0) o[(size_t)i * C] = dcur;
-        slope_prev = slope;
-        yi = ynext;
-        ynext = yafter;
-        dprev = dcur;
-    }
-    real snext = real(0);
-    float spart = 0.0f;
-#pragma unroll 4
-    for (int i = ie - 1; i >= i0; --i) {
-        const real d = (i >= i1) ? halo[(i - i1) * kSolveThreads + threadIdx.x] : o[(size_t)i * C];
-        const real sol = fmad_(-f[i].cp, snext, d);
-        if (i < i1) {
-            o[(size_t)i * C] = sol;
-            if (bnd && i < E - 1) {
-                const float ih = magf(f[i].ih);
-                spart = fmaxf(spart, __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih));
+    for (int base = is; base < i1; base += B) {
+        const int nb = min(B, i1 - base);
+        real fm = real(0), flm = real(0), fih = real(0);
+        if (lane < nb) {
+            const Fac<real> fr = f[base + lane];
+            fm = fr.m;
+            flm = fr.lm;
+            fih = fr.ih;
+        }
+        real yb[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) yb[k] = (k < nb && base + 1 + k < E) ? y[(size_t)(base + 1 + k) * C] : real(0);
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            const real m = shfl_idx_(fm, k), lm = shfl_idx_(flm, k), ih = shfl_idx_(fih, k);
+            if (k < nb) {
+                const int i = base + k;
+                const real ynext = yb[k];
+                real slope = real(0), r = real(0);
+                if (i < E - 1) slope = mul_(sub_(ynext, yi), ih);
+                if (i > 0 && i < E - 1) r = mul_(real(3), sub_(slope, slope_prev));
+                const real dcur = fmad_(-lm, dprev, mul_(m, r));
+                // rows before i0 only warm the recurrence up
+                if (i >= i0) {
+                    if (cok) o[(size_t)i * C] = dcur;
+                    ymax = fmaxf(ymax, magf(yi));
+                }
+                slope_prev = slope;
+                yi = ynext;
+                dprev = dcur;
             }
         }
-        snext = sol;
     }
-    if (bnd) atomicMax(&bnd[c], __float_as_uint((ymax + spart) * 1.01f));
+    if (bnd && cok) {
+        if (i1 < E) ymax = fmaxf(ymax, magf(yi));  // right end of the last piece
+        atomicMax(&bnd[it.c], __float_as_uint(ymax * 1.01f));
+    }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(kSolveThreads)
+k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, const real* __restrict__ dbuf,
+            real* __restrict__ sv, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
+            unsigned* __restrict__ bnd)
+{
+    constexpr int B = kSolveBatch;
+    const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
+    if (!it.ok) return;
+    const int lane = threadIdx.x & 31;
+    const int C = g.C, E = it.E, i0 = it.i0, i1 = it.i1;
+    const bool cok = it.c < C;
+    const int cl = min(it.c, C - 1);
+    const size_t slot = (size_t)it.env * Kc + it.kk;
+    const Fac<real>* f = fac + slot * g.cap;
+    const real* d = dbuf + slot * (size_t)g.cap * C + cl;
+    real* o = sv + slot * (size_t)g.cap * C + cl;
+    const int ie = (H < 0) ? E : min(E, i1 + H);
+    real snext = real(0);
+    float spart = 0.0f;
+    for (int top = ie - 1; top >= i0; top -= B) {
+        const int nb = min(B, top - i0 + 1);
+        real fcp = real(0), fih = real(0);
+        if (lane < nb) {
+            const Fac<real> fr = f[top - lane];
+            fcp = fr.cp;
+            fih = fr.ih;
+        }
+        real db[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) db[k] = (k < nb) ? d[(size_t)(top - k) * C] : real(0);
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+            const real cp = shfl_idx_(fcp, k), ihr = shfl_idx_(fih, k);
+            if (k < nb) {
+                const int i = top - k;
+                const real sol = fmad_(-cp, snext, db[k]);
+                if (i < i1) {
+                    if (cok) o[(size_t)i * C] = sol;
+                    if (bnd && i < E - 1) {
+                        const float ih = magf(ihr);
+                        spart = fmaxf(spart, __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih));
+                    }
+                }
+                snext = sol;
+            }
+        }
+    }
+    if (bnd && cok) atomicMax(&bnd[C + it.c], __float_as_uint(spart * 1.01f));
 }
 
 // ---------------------------------------------------------------------------
@@ -788,7 +868,8 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
 //
 // All anchors, impulses and the recurrence are integers in units of
 // q = 2^(e - 62), 2^e > 2 Kc B_c, with B_c a bound on |S_e(n)| for channel c
-// written by the solve (max |y| + h^2 (|s_i| + |s_{i+1}|) / 4 over the pieces):
+// written by the solve (max |y| plus max h^2 (|s_i| + |s_{i+1}|) / 4 over the
+// pieces):
 // the sums are exact and independent of the order of the directions.  The
 // double-float inputs carry ~48 bits, and the recurrence extrapolates each
 // anchor over at most 16 samples, which keeps the mean within ~1e-13 of its
@@ -832,7 +913,7 @@ k_mean_cum(float2* __restrict__ X, dd* __restrict__ acc_buf, const uint32_t* __r
     for (int i = threadIdx.x; i < 32 * G; i += blockDim.x) imp[i] = 0ull;
     for (int i = threadIdx.x; i < 6 * G; i += blockDim.x) anc[i] = 0ull;
     if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)
-        for (int i = threadIdx.x; i < C; i += blockDim.x) bnd_clear[i] = 0u;
+        for (int i = threadIdx.x; i < 2 * C; i += blockDim.x) bnd_clear[i] = 0u;
     if (warp == 0) {
         int q = 0;
         for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
@@ -840,7 +921,7 @@ k_mean_cum(float2* __restrict__ X, dd* __restrict__ acc_buf, const uint32_t* __r
         if (lane == 0) sQ = q;
     }
     // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex
-    const float B = __uint_as_float(bnd[cl]);
+    const float B = __uint_as_float(bnd[cl]) + __uint_as_float(bnd[C + cl]);
     const bool bad = !(B < INFINITY);
     int ex = 0;
     frexpf(__fmul_rn(B, (float)(2 * Kc)) * 1.0009765625f, &ex);

@@ -74,6 +74,8 @@ struct memd_plan {
     void* rtab;
     void* rtab3;  // impulse-accumulation mean: 1/(3h) as double-float
     unsigned* bnd;  // impulse-accumulation mean: [2 passes][2 parts][C] per-channel bounds (float bits)
+    int* cumcfg;    // impulse-accumulation mean: anchor span (words) and CTAs per span, set by the factor kernel
+    memd::CumShared cumsh;  // impulse-accumulation mean: accumulators of spans split over CTAs
     void* M;     // stop mode: mean envelope of the last pass [L][C]
     void* part;  // stop mode: per channel group, direction and sample sum of (U-L)^2
     void* amp;   // stop mode: amplitude statistic [L]
@@ -174,10 +176,12 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
                 unsigned* other = p->bnd + (size_t)((p->bpass + 1) & 1) * 2 * g.C;
 #define MEMD_CASE(G_)                                                                                              \
     if (p->cumG == G_) {                                                                                           \
-        dim3 grid((unsigned)g.W, (unsigned)((g.C + G_ - 1) / G_));                                                 \
-        k_mean_cum<G_><<<grid, 256, 0, s>>>((float2*)p->X, (dd*)p->acc, p->bits, p->wpref, p->knots, p->cnt,     \
+        dim3 grid((unsigned)((g.W + kCumMaxWords - 1) / kCumMaxWords * kCumMaxWords),                             \
+                  (unsigned)((g.C + G_ - 1) / G_));                                                                \
+        k_mean_cum<G_><<<grid, 256, sizeof(unsigned long long) * (32 * kCumMaxWords + 3) * G_, s>>>((float2*)p->X, (dd*)p->acc, p->bits, p->wpref, p->knots, p->cnt,     \
                                             (const dd*)p->rtab, (const dd*)p->rtab3, (const dd*)p->sv,           \
-                                            (const dd*)p->yv, cur, other, g, k0, kc, first, last, p->st);        \
+                                            (const dd*)p->yv, cur, other, p->cumcfg, p->cumsh, g, k0, kc, first,  \
+                                            last, p->st);                                                          \
         return;                                                                                                    \
     }
                 MEMD_CASE(32) MEMD_CASE(16) MEMD_CASE(8)
@@ -231,6 +235,16 @@ static cudaError_t set_attrs(memd_plan* p)
 #undef MEMD_CASE
     }
     if (e != cudaSuccess) return e;
+    if constexpr (P == MEMD_PREC_MIXED) {
+        const int cb[3] = {32, 16, 8};
+        for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+            const int bytes = (int)sizeof(unsigned long long) * (32 * kCumMaxWords + 3) * cb[i];
+            if (cb[i] == 32) e = cudaFuncSetAttribute(k_mean_cum<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (cb[i] == 16) e = cudaFuncSetAttribute(k_mean_cum<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (cb[i] == 8) e = cudaFuncSetAttribute(k_mean_cum<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        }
+    }
+    if (e != cudaSuccess) return e;
     if constexpr (P == MEMD_PREC_MIXED)
         e = cudaFuncSetAttribute(k_project_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->proj_smem);
     else
@@ -268,7 +282,8 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         const long nf = 2L * kc * nsegf;
         lc.begin();
         k_factor<R><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
-                                                                 (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf);
+                                                                 (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
+                                                                 p->cum ? p->cumcfg : nullptr);
         lc.end(MEMD_STAGE_FACTOR);
         const long nseg = (p->H < 0) ? 1 : (g.cap + p->Ss - 1) / p->Ss;
         const long ns = 2L * kc * nseg * p->ngroups * 32;
@@ -743,6 +758,10 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     if (p->cum) {
         ALLOC(p->rtab3, sizeof(dd) * (size_t)(L + 1));
         ALLOC(p->bnd, sizeof(unsigned) * 4 * (size_t)C);
+        ALLOC(p->cumcfg, sizeof(int) * 4);
+        ALLOC(p->cumsh.kq, sizeof(unsigned long long) * 35 * (size_t)p->g.W * C);
+        ALLOC(p->cumsh.anc, sizeof(unsigned long long) * 4 * (size_t)p->g.W * C);
+        ALLOC(p->cumsh.arrive, sizeof(int) * (size_t)p->g.W * ((C + 7) / 8));
     }
     if (c.stop_mode == MEMD_STOP_CRITERION) {
         ALLOC(p->M, rb * CL);
@@ -781,6 +800,12 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         cudaFree(r64);
         cudaFree(r32);
         cudaFree(rdd);
+    }
+    if (e == cudaSuccess && p->cum) {
+        e = cudaMemset(p->cumsh.kq, 0, sizeof(unsigned long long) * 35 * (size_t)p->g.W * C);
+        if (e == cudaSuccess) e = cudaMemset(p->cumsh.anc, 0, sizeof(unsigned long long) * 4 * (size_t)p->g.W * C);
+        if (e == cudaSuccess) e = cudaMemset(p->cumsh.arrive, 0, sizeof(int) * (size_t)p->g.W * ((C + 7) / 8));
+        if (e == cudaSuccess) e = cudaMemset(p->cumcfg, 0, sizeof(int) * 4);
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {

@@ -243,8 +243,34 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
 template <typename real>
 __global__ void __launch_bounds__(128)
 k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real* __restrict__ rtab,
-         Fac<real>* __restrict__ fac, Geom g, int k0, int Kc, int Sf, int Hf)
+         Fac<real>* __restrict__ fac, Geom g, int k0, int Kc, int Sf, int Hf, int* __restrict__ cumcfg)
 {
+    // cumcfg != nullptr (impulse-accumulation mean): block 0 picks the mean
+    // kernel's anchor span, 32 m samples (m the largest power of two <= 8 with
+    // 32 m <= 9 h, h the chunk's mean knot spacing), and splits each span's
+    // (direction, envelope) pairs over P = m CTAs
+    if (cumcfg && blockIdx.x == 0 && threadIdx.x < 32) {
+        int q = 0;
+        long long et = 0;
+        for (int k = threadIdx.x; k < Kc; k += 32) {
+            const int a = cnt[k0 + k], b = cnt[g.K + k0 + k];
+            if (a > 3 && b > 3) {
+                ++q;
+                et += a + b;
+            }
+        }
+        q = warp_sum(q);
+        et = warp_sum(et);
+        if (threadIdx.x == 0) {
+            int m = 1;
+            if (et > 0) {
+                const double h = (double)g.L * (2.0 * q) / (double)et;
+                while (m < 8 && 32.0 * (2 * m) <= 9.0 * h) m *= 2;
+            }
+            cumcfg[0] = m;
+            cumcfg[1] = m;
+        }
+    }
     const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nseg = (g.cap + Sf - 1) / Sf;
     const int seg = (int)(gid % nseg);
@@ -860,179 +886,384 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
 // (n - x)_+^3 is 1, 4, 1 at n = x-3, x-2, x-1 and zero elsewhere, so the sum
 // over all envelopes M(n) = sum_e S_e(n) obeys
 //     Delta^4 M(n) = I(n) = sum over interior knots of dd_j * {1,4,1}.
-// Per 32-sample word the kernel anchors M at the middle sample n_a (value and
-// the first three forward differences of the pieces active there, plus the
-// impulses that knots at n_a+1, n_a+2 place before n_a), then rebuilds M(n)
-// by running the difference recurrence forwards and backwards over the word.
-// Work per word: O(knots + envelopes) instead of O(envelopes x samples).
+// Per span of 32 m samples (m = 1 .. 8 words, longer where the knots are
+// sparse) the kernel anchors M at the middle sample n_a (value and the first
+// three forward differences of the pieces active there, plus the impulses that
+// knots at n_a+1, n_a+2 place before n_a), then rebuilds M(n) by running the
+// difference recurrence forwards and backwards over the span.  Work per span:
+// O(knots + envelopes) instead of O(envelopes x samples).
 //
-// All anchors, impulses and the recurrence are integers in units of
-// q = 2^(e - 62), 2^e > 2 Kc B_c, with B_c a bound on |S_e(n)| for channel c
-// written by the solve (max |y| plus max h^2 (|s_i| + |s_{i+1}|) / 4 over the
-// pieces):
-// the sums are exact and independent of the order of the directions.  The
+// The jumps q_j - q_{j-1} (q_j: d_j quantised), the anchor sums and the
+// recurrence are integers in units of q = 2^(e - 62), 2^e > 2 Kc B_c, with B_c
+// a bound on |S_e(n)| for channel c written by the solve (max |y| plus max
+// h^2 (|s_i| + |s_{i+1}|) / 4 over the pieces), so the sums over directions
+// are exact and independent of their order; each lane's anchor coefficients
+// are summed in double-float in a fixed order before quantisation.  The
 // double-float inputs carry ~48 bits, and the recurrence extrapolates each
-// anchor over at most 16 samples, which keeps the mean within ~1e-13 of its
-// value relative to the signal (the direct evaluation: ~1e-15).
+// anchor over at most 16 m samples, 16 m <= 4.5 mean knot spacings, which keeps
+// the mean within ~1e-13 of its value relative to the signal (the direct
+// evaluation: ~1e-15).
 //
-// CTA: one word x G channels, 8 warps; lane = (subgroup, channel), the
-// (direction, envelope) pairs are dealt round-robin to the 8 * 32/G
-// subgroups, whose impulses meet in shared memory (64-bit integer atomics).
-// Warp 0 then runs the forward half of the recurrence, warp 1 the backward.
+// CTA: one span (or one of the P parts of a span's directions) x G channels,
+// 8 warps; lane = (subgroup, channel), the (direction,
+// envelope) pairs are dealt round-robin to the 8 * 32/G subgroups, which add
+// each knot's jump into a per-row array in shared memory (one 64-bit integer
+// atomic per knot).  The recurrence runs as four block-wide exact prefix sums
+// plus the cubic that matches the anchor state, so all warps share it.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long qfix(dd v, float sc)
+// The double-float v times 2^sh as a 64-bit two's-complement integer (|v 2^sh|
+// < 2^62; bits below the 48-bit combined mantissa are dropped), by integer
+// instructions only: the float-to-int64 conversion instructions run on the
+// FP64 pipe, 1/64 of the FP32 rate on this GPU.
+__device__ __forceinline__ unsigned long long qfix(dd v, int sh)
 {
-    return (unsigned long long)__float2ll_rn(__fmul_rn(v.hi, sc)) +
-           (unsigned long long)__float2ll_rn(__fmul_rn(v.lo, sc));
+    const unsigned uh = __float_as_uint(v.hi), ul = __float_as_uint(v.lo);
+    const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
+    if (eh == 0) return 0ull;  // zero (or subnormal): below any quantum in use
+    int mh = (int)((uh & 0x7fffffu) | 0x800000u);
+    int ml = (el == 0) ? 0 : (int)((ul & 0x7fffffu) | 0x800000u);
+    if (uh >> 31) mh = -mh;
+    if (ul >> 31) ml = -ml;
+    // lo in units of 2^(eh - 174): ml 2^(el - eh + 24); |lo| <= ulp(hi) gives el <= eh - 23
+    const int dl = eh - el - 24;
+    const int mlo = (dl < 0) ? ml * 2 : (dl < 31 ? (ml >> dl) : (ml < 0 ? -1 : 0));
+    const long long comb = (long long)mh * (1ll << 24) + (long long)mlo;  // |comb| < 2^48
+    const int s = eh - 174 + sh;                                           // value 2^sh = comb 2^s
+    const long long r = (s >= 0) ? (long long)((unsigned long long)comb << min(s, 63))
+                                 : (comb >> min(-s, 63));
+    return (unsigned long long)r;
 }
 
+// the non-negative integer a (< 2^63) times 2^-sh as a float, truncated to
+// 24 bits; *rest receives the bits below them
+__device__ __forceinline__ float fix2f(unsigned long long a, int sh, unsigned long long* rest)
+{
+    if (a == 0ull) {
+        *rest = 0ull;
+        return 0.0f;
+    }
+    const int msb = 63 - __clzll((long long)a);
+    const int sd = msb - 23;
+    const unsigned long long top = (sd >= 0) ? (a >> sd) : (a << -sd);
+    *rest = (sd > 0) ? a - (top << sd) : 0ull;
+    const int be = msb - sh + 127;  // biased exponent of the result
+    if (be <= 0) return 0.0f;
+    return __uint_as_float(((unsigned)be << 23) | ((unsigned)top & 0x7fffffu));
+}
+// the two's-complement integer v times 2^-sh as a double-float (~47 bits)
+__device__ __forceinline__ dd fix2dd(unsigned long long v, int sh)
+{
+    const bool neg = (long long)v < 0;
+    const unsigned long long a = neg ? 0ull - v : v;
+    unsigned long long r1, r2;
+    const float hi = fix2f(a, sh, &r1);
+    const float lo = fix2f(r1, sh, &r2);
+    return neg ? dd(-hi, -lo) : dd(hi, lo);
+}
+
+constexpr int kCumMaxWords = 8;  // longest anchor span: 8 words = 256 samples
+constexpr int kCumMaxParts = 8;  // most CTAs sharing one span
+
+// Global accumulators of the spans split over several CTAs (zero between
+// launches: the CTA that finishes a span clears them).
+struct CumShared {
+    unsigned long long* kq;   // [W][35][C]: span si uses rows si*(32m+3) .. (si+1)*(32m+3)-1
+    unsigned long long* anc;  // [W][4][C]
+    int* arrive;              // [groups][W]
+};
+
 template <int G>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 k_mean_cum(float2* __restrict__ X, dd* __restrict__ acc_buf, const uint32_t* __restrict__ bits,
            const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
            const dd* __restrict__ rtab, const dd* __restrict__ rtab3, const dd* __restrict__ sv,
-           const dd* __restrict__ yv, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear, Geom g,
-           int k0, int Kc, int first_chunk, int last_chunk, RunState* st)
+           const dd* __restrict__ yv, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear,
+           const int* __restrict__ cumcfg, CumShared sh_g, Geom g, int k0, int Kc, int first_chunk, int last_chunk,
+           RunState* st)
 {
     constexpr int SUB = 32 / G;
     constexpr int NWS = 8 * SUB;
-    __shared__ unsigned long long imp[32 * G];
-    __shared__ unsigned long long anc[6 * G];
-    __shared__ int sQ;
+    constexpr int NE = 256;  // (direction, envelope) pairs described per round
+    constexpr int KB = 4;    // knots per batch of loads
+    extern __shared__ __align__(16) unsigned long long kq[];  // [32 * kCumMaxWords + 3][G]: jump of d at row x - p0
+    __shared__ unsigned long long anc[4 * G];
+    __shared__ unsigned long long part[NWS * G];  // per row group: totals of a scan pass
+    __shared__ unsigned long long pst[6 * G];     // particular solution at n_a; look-ahead jumps
+    __shared__ int eI[NE], eJ[NE], eN[NE], eX[NE], eH[NE];
+    __shared__ int sQ, sLast;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cc = lane % G, sub = lane / G;
-    const int w = blockIdx.x;
-    const int p0 = w * 32;
-    const int nl = min(32, g.L - p0);
-    const int ra = min(16, nl - 1);
-    const int na = p0 + ra;
     const int C = g.C;
+    const int mw = min(max(cumcfg[0], 1), kCumMaxWords), P = min(max(cumcfg[1], 1), kCumMaxParts);
+    // CTA b works on part b % P of span b / P (launched: W rounded up to a
+    // multiple of 8 CTAs, so that every part of every span exists; P = m | 8)
+    const int si = blockIdx.x / P, prt = blockIdx.x % P;
+    const int w = si * mw;
+    if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)
+        for (int i = threadIdx.x; i < 2 * C; i += blockDim.x) bnd_clear[i] = 0u;
+    if (w >= g.W) return;  // uniform over the CTA
+    const int p0 = w * 32;
+    const int nl = min(32 * mw, g.L - p0);
+    const int ra = min(16 * mw, nl - 1);
+    const int na = p0 + ra;
     const int c = blockIdx.y * G + cc;
     const bool cok = c < C;
     const int cl = min(c, C - 1);  // loads of lanes past the last channel stay in bounds
-    for (int i = threadIdx.x; i < 32 * G; i += blockDim.x) imp[i] = 0ull;
-    for (int i = threadIdx.x; i < 6 * G; i += blockDim.x) anc[i] = 0ull;
-    if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)
-        for (int i = threadIdx.x; i < 2 * C; i += blockDim.x) bnd_clear[i] = 0u;
-    if (warp == 0) {
-        int q = 0;
-        for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
-        q = warp_sum(q);
-        if (lane == 0) sQ = q;
-    }
+    for (int i = threadIdx.x; i < (nl + 3) * G; i += blockDim.x) kq[i] = 0ull;
+    for (int i = threadIdx.x; i < 4 * G; i += blockDim.x) anc[i] = 0ull;
     // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex
     const float B = __uint_as_float(bnd[cl]) + __uint_as_float(bnd[C + cl]);
     const bool bad = !(B < INFINITY);
     int ex = 0;
     frexpf(__fmul_rn(B, (float)(2 * Kc)) * 1.0009765625f, &ex);
     ex = max(ex, -60);
-    const float sc = ldexpf(1.0f, 62 - ex);  // value -> units
-    const float qv = ldexpf(1.0f, ex - 62);  // units -> value
+    const int sh = 62 - ex;  // value = units * 2^-sh
     const dd third = dd(1.0 / 3.0);
-    __syncthreads();
+    const int wa = w + (ra >> 5), ba = ra & 31;
+    const int wend = min(w + mw, g.W);
+    // this CTA's share of the (direction, envelope) pairs
+    const int e_lo = (int)((long)prt * 2 * Kc / P), e_hi = (int)((long)(prt + 1) * 2 * Kc / P);
 
-    unsigned long long aA = 0, aB = 0, aC = 0, aD = 0, la2 = 0, la3 = 0;
-    const int xend = p0 + nl + 2;  // knots up to here place impulses in the word
-    for (int ei = warp * SUB + sub; ei < 2 * Kc; ei += NWS) {
-        const int kk = ei >> 1, env = ei & 1;
-        const int k = k0 + kk;
-        const int Ex = cnt[k], En = cnt[g.K + k];
-        if (!(Ex > 3 && En > 3) || Ex > g.cap || En > g.cap) continue;
-        const int E = env ? En : Ex;
-        const size_t slot = (size_t)env * Kc + kk;
-        const uint32_t bw = bits[slot * g.W + w];
-        const int wp = wpref[slot * (g.W + 1) + w];
-        const int* kn = knots + slot * g.cap;
-        const dd* sc_ = sv + slot * (size_t)g.cap * C + cl;
-        const dd* yc_ = yv + slot * (size_t)g.cap * C + cl;
-        // anchor: the piece [x_i, x_{i+1}] with x_i <= n_a < x_{i+1}
+    dd aA(0.0f, 0.0f), aB(0.0f, 0.0f), aC(0.0f, 0.0f), aD(0.0f, 0.0f);  // anchor coefficients, summed in a fixed order
+    for (int base = e_lo; base < e_hi; base += NE) {
+        __syncthreads();
+        // (1) per (direction, envelope): anchor piece i (x_i <= n_a < x_{i+1}),
+        //     first interior knot j past p0 and the number n of interior knots
+        //     in (p0, p0 + nl + 2]; n = -1 marks a direction that does not count
         {
-            const uint32_t le = (ra == 31) ? bw : (bw & ((2u << ra) - 1u));
-            const int i = min(wp + __popc(le) - 1, E - 2);
-            const int xi = kn[i], h = kn[i + 1] - xi;
-            const dd y0 = yc_[(size_t)i * C], y1 = yc_[(size_t)(i + 1) * C];
-            const dd s0 = sc_[(size_t)i * C], s1 = sc_[(size_t)(i + 1) * C];
-            const dd d = (s1 - s0) * rtab3[h];
-            const dd b = (y1 - y0) * rtab[h] - dd_mulf(dd_mulf(s0, 2.0f) + s1, (float)h) * third;
-            const float u = (float)(na - xi);
-            const dd d3 = dd_mulf(d, 3.0f);
-            aA += qfix(dd_mulf(dd_mulf(dd_mulf(d, u) + s0, u) + b, u) + y0, sc);
-            aB += qfix(dd_mulf(dd_mulf(d3, u) + dd_mulf(s0, 2.0f), u) + b, sc);
-            aC += qfix(dd_mulf(d3, u) + s0, sc);
-            aD += qfix(d, sc);
+            const int ei = base + (int)threadIdx.x;
+            int n = -1, i = 0, j = 0, xi = 0, hh = 1;
+            if (ei < e_hi) {
+                const int kk = ei >> 1, env = ei & 1, k = k0 + kk;
+                const int Ex = cnt[k], En = cnt[g.K + k];
+                if (Ex > 3 && En > 3 && Ex <= g.cap && En <= g.cap) {
+                    const int E = env ? En : Ex;
+                    const size_t slot = (size_t)env * Kc + kk;
+                    const uint32_t* bb = bits + slot * g.W;
+                    const int* wp = wpref + slot * (g.W + 1);
+                    const uint32_t bw = bb[w];
+                    const uint32_t bwa = bb[wa];
+                    const uint32_t le = (ba == 31) ? bwa : (bwa & ((2u << ba) - 1u));
+                    i = min(wp[wa] + __popc(le) - 1, E - 2);
+                    j = max(1, wp[w] + (int)(bw & 1u));
+                    int nw = wp[wend] - wp[w] - (int)(bw & 1u);  // knots in (p0, p0 + 32 m)
+                    if (wend < g.W && nl == 32 * mw) nw += __popc(bb[wend] & 7u);
+                    n = max(0, min(j + nw - 1, E - 2) - j + 1);
+                    const int* kn = knots + slot * g.cap;
+                    xi = kn[i];
+                    hh = kn[i + 1] - xi;
+                }
+            }
+            if (threadIdx.x < NE) {
+                eI[threadIdx.x] = i;
+                eJ[threadIdx.x] = j;
+                eN[threadIdx.x] = n;
+                eX[threadIdx.x] = xi;
+                eH[threadIdx.x] = hh;
+            }
         }
-        // impulses of the interior knots x_j in (p0, p0 + nl + 2]
-        int j = max(1, wp + (int)(bw & 1u));
-        if (j <= E - 2) {
-            int xj = kn[j];
-            if (xj <= xend) {
-                const int xp = kn[j - 1];
-                dd scur = sc_[(size_t)j * C];
-                dd dprev = (scur - sc_[(size_t)(j - 1) * C]) * rtab3[xj - xp];
-                for (;;) {
-                    const int xn = kn[j + 1];
-                    const dd sn = sc_[(size_t)(j + 1) * C];
-                    const dd dcur = (sn - scur) * rtab3[xn - xj];
-                    const unsigned long long qd = qfix(dcur - dprev, sc);
-                    const int r = xj - 3 - p0;
-                    if (r >= 0 && r < nl) atomicAdd(&imp[r * G + cc], qd);
-                    if (r + 1 >= 0 && r + 1 < nl) atomicAdd(&imp[(r + 1) * G + cc], qd << 2);
-                    if (r + 2 >= 0 && r + 2 < nl) atomicAdd(&imp[(r + 2) * G + cc], qd);
-                    if (xj == na + 1) {
-                        la2 += qd;
-                        la3 += 5ull * qd;
-                    } else if (xj == na + 2) {
-                        la3 += qd;
+        __syncthreads();
+        const int nround = min(NE, e_hi - base);
+        for (int le = warp * SUB + sub; le < nround; le += NWS) {
+            const int n = eN[le];
+            if (n < 0) continue;
+            const int ei = base + le;
+            const int kk = ei >> 1, env = ei & 1;
+            const size_t slot = (size_t)env * Kc + kk;
+            const int* kn = knots + slot * g.cap;
+            const size_t rb = slot * (size_t)g.cap * C + cl;
+            // (2) anchor: Taylor coefficients of the piece at n_a
+            {
+                const int i = eI[le];
+                const int xi = eX[le], h = eH[le];
+                const dd y0 = yv[rb + (size_t)i * C], y1 = yv[rb + (size_t)(i + 1) * C];
+                const dd s0 = sv[rb + (size_t)i * C], s1 = sv[rb + (size_t)(i + 1) * C];
+                const dd d = (s1 - s0) * rtab3[h];
+                const dd s02(2.0f * s0.hi, 2.0f * s0.lo);  // exact
+                const dd b = (y1 - y0) * rtab[h] - dd_mulf(s02 + s1, (float)h) * third;
+                const float u = (float)(na - xi);
+                const dd d3 = dd_mulf(d, 3.0f);
+                aA = aA + (dd_mulf(dd_mulf(dd_mulf(d, u) + s0, u) + b, u) + y0);
+                aB = aB + (dd_mulf(dd_mulf(d3, u) + s02, u) + b);
+                aC = aC + (dd_mulf(d3, u) + s0);
+                aD = aD + d;
+            }
+            // (3) jumps q_j - q_{j-1} at row x_j - p0 (in 1 .. nl + 2), q_j the
+            //     quantised d_j = (s_{j+1} - s_j) / (3 h_j); batches of KB knots
+            const int j0 = eJ[le];
+            if (n > 0) {
+                int xj = kn[j0];
+                dd sj = sv[rb + (size_t)j0 * C];
+                unsigned long long qprev = qfix((sj - sv[rb + (size_t)(j0 - 1) * C]) * rtab3[xj - kn[j0 - 1]], sh);
+                for (int t0 = 0; t0 < n; t0 += KB) {
+                    const int nb = min(KB, n - t0);
+                    int xn[KB];
+                    dd sn[KB], r3[KB];
+#pragma unroll
+                    for (int k = 0; k < KB; ++k) {
+                        if (k < nb) {
+                            xn[k] = kn[j0 + t0 + k + 1];
+                            sn[k] = sv[rb + (size_t)(j0 + t0 + k + 1) * C];
+                        }
                     }
-                    ++j;
-                    if (j > E - 2 || xn > xend) break;
-                    xj = xn;
-                    scur = sn;
-                    dprev = dcur;
+                    {
+                        int xa = xj;
+#pragma unroll
+                        for (int k = 0; k < KB; ++k) {
+                            if (k < nb) {
+                                r3[k] = rtab3[xn[k] - xa];
+                                xa = xn[k];
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < KB; ++k) {
+                        if (k < nb) {
+                            const unsigned long long qcur = qfix((sn[k] - sj) * r3[k], sh);
+                            atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
+                            qprev = qcur;
+                            xj = xn[k];
+                            sj = sn[k];
+                        }
+                    }
                 }
             }
         }
     }
-    atomicAdd(&anc[0 * G + cc], aA);
-    atomicAdd(&anc[1 * G + cc], aB);
-    atomicAdd(&anc[2 * G + cc], aC);
-    atomicAdd(&anc[3 * G + cc], aD);
-    atomicAdd(&anc[4 * G + cc], la2);
-    atomicAdd(&anc[5 * G + cc], la3);
+    atomicAdd(&anc[0 * G + cc], qfix(aA, sh));
+    atomicAdd(&anc[1 * G + cc], qfix(aB, sh));
+    atomicAdd(&anc[2 * G + cc], qfix(aC, sh));
+    atomicAdd(&anc[3 * G + cc], qfix(aD, sh));
+    __syncthreads();
+    if (P > 1) {
+        // a span shared by P CTAs: add this CTA's rows to the span's global
+        // accumulators; the last CTA to arrive finishes the span and clears them
+        const int rows = 32 * mw + 3;
+        unsigned long long* gk = sh_g.kq + (size_t)si * rows * C + (size_t)blockIdx.y * G;
+        unsigned long long* ga = sh_g.anc + (size_t)si * 4 * C + (size_t)blockIdx.y * G;
+        for (int i = threadIdx.x; i < (nl + 3) * G; i += blockDim.x) {
+            const int r = i / G, ch = i - r * G;
+            const unsigned long long v = kq[i];
+            if (v != 0ull && blockIdx.y * G + ch < C) atomicAdd(&gk[(size_t)r * C + ch], v);
+        }
+        for (int i = threadIdx.x; i < 4 * G; i += blockDim.x) {
+            const int r = i / G, ch = i - r * G;
+            if (blockIdx.y * G + ch < C) atomicAdd(&ga[(size_t)r * C + ch], anc[i]);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) sLast = (atomicAdd(&sh_g.arrive[(size_t)blockIdx.y * g.W + si], 1) == P - 1);
+        __syncthreads();
+        if (!sLast) return;  // uniform over the CTA
+        __threadfence();
+        for (int i = threadIdx.x; i < (nl + 3) * G; i += blockDim.x) {
+            const int r = i / G, ch = i - r * G;
+            unsigned long long v = 0ull;
+            if (blockIdx.y * G + ch < C) {
+                v = __ldcg(&gk[(size_t)r * C + ch]);
+                gk[(size_t)r * C + ch] = 0ull;
+            }
+            kq[i] = v;
+        }
+        for (int i = threadIdx.x; i < 4 * G; i += blockDim.x) {
+            const int r = i / G, ch = i - r * G;
+            unsigned long long v = 0ull;
+            if (blockIdx.y * G + ch < C) {
+                v = __ldcg(&ga[(size_t)r * C + ch]);
+                ga[(size_t)r * C + ch] = 0ull;
+            }
+            anc[i] = v;
+        }
+        if (threadIdx.x == 0) sh_g.arrive[(size_t)blockIdx.y * g.W + si] = 0;
+    }
+    if (warp == 0) {
+        int q = 0;
+        for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        q = warp_sum(q);
+        if (lane == 0) sQ = q;
+    }
+    // (4) M over the span, in parallel: row group rg = warp * SUB + sub owns
+    //     rows [r0, r1).  The particular solution P (zero state at row 0) is
+    //     four exclusive prefix sums of the impulses I(r) = kq[r+1] + 4 kq[r+2]
+    //     + kq[r+3]; M = P + H with H the cubic (Delta^4 H = 0) whose
+    //     differences at n_a are the anchor state minus P's.
+    const int rg = warp * SUB + sub;
+    const int RB = (nl + NWS - 1) / NWS;
+    const int r0 = min(nl, rg * RB), r1 = min(nl, r0 + RB);
+    unsigned long long e0 = 0, e1 = 0, e2 = 0;  // rows r1 .. r1 + 2, read before they are overwritten
+    __syncthreads();
+    if (r0 < r1) {
+        e0 = kq[r1 * G + cc];
+        e1 = kq[(r1 + 1) * G + cc];
+        e2 = kq[(r1 + 2) * G + cc];
+    }
+    if (rg == 0) {
+        pst[3 * G + cc] = kq[(ra + 1) * G + cc];  // jump at n_a + 1
+        pst[4 * G + cc] = kq[(ra + 2) * G + cc];  // jump at n_a + 2
+    }
     __syncthreads();
     const int Q = sQ;
     if (last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
-    if (warp >= 2 || sub != 0 || !cok) return;
-    const unsigned long long sA = anc[cc], sB = anc[G + cc], sC = anc[2 * G + cc], sD = anc[3 * G + cc];
-    unsigned long long v = sA, d1 = sB + sC + sD, d2 = 2ull * sC + 6ull * sD + anc[4 * G + cc],
-                       d3 = 6ull * sD + anc[5 * G + cc];
-    const dd qd = dd((float)Q, 0.0f);
-    auto emit = [&](int r, unsigned long long val) {
-        const long long vi = (long long)val;
-        const float hi = __ll2float_rn(vi);
-        const float lo = __ll2float_rn(vi - __float2ll_rn(hi));
-        dd tot(__fmul_rn(hi, qv), __fmul_rn(lo, qv));
-        if (bad) tot = dd(__int_as_float(0x7fc00000), 0.0f);
-        const size_t off = (size_t)(p0 + r) * C + c;
-        if (!first_chunk) tot = tot + acc_buf[off];
-        if (last_chunk) X[off] = xsub(X[off], dd_mulf(tot, 0.5f) / qd);
-        else acc_buf[off] = tot;
-    };
-    if (warp == 0) {
-        for (int r = ra; r < nl; ++r) {
-            emit(r, v);
-            v += d1;
-            d1 += d2;
-            d2 += d3;
-            d3 += imp[r * G + cc];
+    for (int r = r0; r < r1; ++r) {  // in place: I(r) reads rows > r only
+        const unsigned long long a1 = (r + 1 < r1) ? kq[(r + 1) * G + cc] : (r + 1 == r1 ? e0 : (r + 1 == r1 + 1 ? e1 : e2));
+        const unsigned long long a2 = (r + 2 < r1) ? kq[(r + 2) * G + cc] : (r + 2 == r1 ? e0 : (r + 2 == r1 + 1 ? e1 : e2));
+        const unsigned long long a3 = (r + 3 < r1) ? kq[(r + 3) * G + cc] : (r + 3 == r1 ? e0 : (r + 3 == r1 + 1 ? e1 : e2));
+        kq[r * G + cc] = a1 + (a2 << 2) + a3;
+    }
+    for (int pass = 0; pass < 4; ++pass) {
+        unsigned long long run = 0;
+        for (int r = r0; r < r1; ++r) {
+            const unsigned long long t = kq[r * G + cc];
+            kq[r * G + cc] = run;
+            run += t;
         }
-    } else {
-        for (int r = ra - 1; r >= 0; --r) {
-            d3 -= imp[r * G + cc];
-            d2 -= d3;
-            d1 -= d2;
-            v -= d1;
-            emit(r, v);
+        part[rg * G + cc] = run;
+        __syncthreads();
+        unsigned long long off = 0;
+        for (int q = 0; q < rg; ++q) off += part[q * G + cc];
+        for (int r = r0; r < r1; ++r) kq[r * G + cc] += off;
+        if (pass < 3 && ra >= r0 && ra < r1) pst[pass * G + cc] = kq[ra * G + cc];  // P's d3, d2, d1 at n_a
+        __syncthreads();
+    }
+    if (!cok || r0 >= r1) return;
+    const unsigned long long sA = anc[cc], sB = anc[G + cc], sC = anc[2 * G + cc], sD = anc[3 * G + cc];
+    const unsigned long long k1 = pst[3 * G + cc], k2 = pst[4 * G + cc];
+    // state at n_a: differences of the anchor polynomials plus the part of the
+    // jumps at n_a + 1 and n_a + 2 that falls before n_a (Delta^4 of (n - x)_+^3
+    // is 1, 4, 1 at x - 3, x - 2, x - 1), minus P's state there
+    const unsigned long long h0 = sA - kq[ra * G + cc];
+    const unsigned long long h1 = sB + sC + sD - pst[2 * G + cc];
+    const unsigned long long h2 = 2ull * sC + 6ull * sD + k1 - pst[1 * G + cc];
+    const unsigned long long h3 = 6ull * sD + 5ull * k1 + k2 - pst[cc];
+    const dd qd = dd((float)Q, 0.0f);
+    constexpr int XB = 4;  // rows per batch of X loads
+    for (int rb0 = r0; rb0 < r1; rb0 += XB) {
+        float2 xs[XB];
+        dd ac[XB];
+#pragma unroll
+        for (int k = 0; k < XB; ++k) {
+            if (rb0 + k < r1) {
+                const size_t off = (size_t)(p0 + rb0 + k) * C + c;
+                if (last_chunk) xs[k] = X[off];
+                if (!first_chunk) ac[k] = acc_buf[off];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < XB; ++k) {
+            const int r = rb0 + k;
+            if (r < r1) {
+                // H(n_a + t) = h0 + t h1 + C(t,2) h2 + C(t,3) h3 (Newton's form, any integer t)
+                const long long t = r - ra;
+                const unsigned long long c2 = (unsigned long long)(t * (t - 1) / 2);
+                const unsigned long long c3 = (unsigned long long)(t * (t - 1) * (t - 2) / 6);
+                const unsigned long long val = kq[r * G + cc] + h0 + (unsigned long long)t * h1 + c2 * h2 + c3 * h3;
+                dd tot = fix2dd(val, sh);
+                if (bad) tot = dd(__int_as_float(0x7fc00000), 0.0f);
+                const size_t off = (size_t)(p0 + r) * C + c;
+                if (!first_chunk) tot = tot + ac[k];
+                if (last_chunk) X[off] = xsub(xs[k], dd_mulf(tot, 0.5f) / qd);
+                else acc_buf[off] = tot;
+            }
         }
     }
 }

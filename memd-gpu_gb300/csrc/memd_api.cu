@@ -63,12 +63,14 @@ struct memd_plan {
     int bpass;                  // (sift, chunk) passes enqueued so far in the decomposition being built
     size_t proj_smem;
     void* X;
+    void* Xb;  // impulse-accumulation mean: the other working-signal buffer (the mean kernel reads X, writes Xb)
     void* run;
     void* dir;   // FP64/FP32: K x C; mixed: high words then low words
     void* acc;
     void* imf;
     void* yv;
     void* sv;
+    void* yend;  // impulse-accumulation mean: clamped end-knot values [2][Kc][2][C] (no yv gather)
     void* dbuf;  // forward-eliminated right-hand sides [2][Kc][cap][C]
     void* fac;
     void* rtab;
@@ -178,9 +180,10 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
     if (p->cumG == G_) {                                                                                           \
         dim3 grid((unsigned)((g.W + kCumMaxWords - 1) / kCumMaxWords * kCumMaxWords),                             \
                   (unsigned)((g.C + G_ - 1) / G_));                                                                \
-        k_mean_cum<G_><<<grid, 256, sizeof(unsigned long long) * (32 * kCumMaxWords + 3) * G_, s>>>((float2*)p->X, (dd*)p->acc, p->bits, p->wpref, p->knots, p->cnt,     \
+        k_mean_cum<G_><<<grid, 256, sizeof(unsigned long long) * (32 * kCumMaxWords + 3) * G_, s>>>(               \
+            (const float2*)p->X, (float2*)p->Xb, (dd*)p->acc, p->bits, p->wpref, p->knots, p->cnt,               \
                                             (const dd*)p->rtab, (const dd*)p->rtab3, (const dd*)p->sv,           \
-                                            (const dd*)p->yv, cur, other, p->cumcfg, p->cumsh, g, k0, kc, first,  \
+                                            (const dd*)p->yend, cur, other, p->cumcfg, p->cumsh, g, k0, kc, first,\
                                             last, p->st);                                                          \
         return;                                                                                                    \
     }
@@ -276,7 +279,8 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.end(MEMD_STAGE_PROJECT);
         lc.begin();
         k_compact<R, XT><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (R*)p->yv,
-                                                            (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows);
+                                                            (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows,
+                                                            p->cum ? (R*)p->yend : nullptr);
         lc.end(MEMD_STAGE_COMPACT);
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
@@ -290,8 +294,10 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         const unsigned nb = (unsigned)((ns + kSolveThreads - 1) / kSolveThreads);
         unsigned* bcur = p->cum ? p->bnd + (size_t)(p->bpass & 1) * 2 * g.C : nullptr;
         lc.begin();
-        k_solve_fwd<R><<<nb, kSolveThreads, 0, s>>>((const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0,
-                                                   kc, p->S, p->Ss, p->H, p->ngroups, bcur);
+        k_solve_fwd<R, XT><<<nb, kSolveThreads, 0, s>>>((const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g,
+                                                       k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
+                                                       p->cum ? (const XT*)p->X : nullptr, p->knots,
+                                                       p->cum ? (const R*)p->yend : nullptr);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         k_solve_bwd<R><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0,
@@ -301,6 +307,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
         lc.end(MEMD_STAGE_EVAL);
         ++p->bpass;
+        if (p->cum && ch == p->nchunks - 1) std::swap(p->X, p->Xb);  // the next pass reads the updated signal
         if (stop) {
             lc.begin();
             k_amp<R><<<(unsigned)((g.L + 255) / 256), 256, 0, s>>>((const R*)p->part, (R*)p->amp, p->cnt, g, k0, kc,
@@ -335,6 +342,7 @@ static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
     const int maxit = (int)p->cfg.max_iter;
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
     p->bpass = 0;
+    void* const x0 = p->X;
     if (p->cum) cudaMemsetAsync(p->bnd, 0, sizeof(unsigned) * 4 * (size_t)g.C, s);
     for (int i = 0; i + 1 < nimf; ++i) {
         cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, s);
@@ -349,6 +357,7 @@ static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
     lc.begin();
     k_to_channel_major<XT, T><<<tg, tb, 0, s>>>((const XT*)p->run, (T*)p->imf + (size_t)(nimf - 1) * CL, nullptr, g.C, g.L);
     lc.end(MEMD_STAGE_OTHER);
+    if (p->X != x0) std::swap(p->X, p->Xb);  // the buffers' roles as at the start
 }
 
 template <int P>
@@ -742,6 +751,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         if (st == MEMD_OK) st = dev_alloc(p, (void**)&(ptr), (bytes)); \
     } while (0)
     ALLOC(p->X, (size_t)p->xbytes * CL);
+    if (p->cum) ALLOC(p->Xb, (size_t)p->xbytes * CL);
     ALLOC(p->run, (size_t)p->xbytes * CL);
     ALLOC(p->dir, 8 * (size_t)K * C);
     if (p->nchunks > 1) ALLOC(p->acc, rb * CL);
@@ -751,7 +761,8 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     ALLOC(p->knots, sizeof(int) * 2 * Kc * p->g.cap);
     ALLOC(p->cnt, sizeof(int) * 2 * (size_t)K);
     ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
-    ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
+    if (!p->cum) ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
+    else ALLOC(p->yend, rb * 2 * Kc * 2 * C);
     ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->dbuf, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->rtab, rb * (size_t)(L + 1));

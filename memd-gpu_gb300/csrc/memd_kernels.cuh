@@ -129,8 +129,12 @@ template <typename real, typename XT>
 __global__ void __launch_bounds__(512)
 k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __restrict__ knots,
           int* __restrict__ cnt, real* __restrict__ yv, const XT* __restrict__ X,
-          memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st, int trace_rows)
+          memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st, int trace_rows,
+          real* __restrict__ yend)
 {
+    // yend != nullptr: the knot values are not gathered; only the two end
+    // knots' values (clamped) are written, to yend[env][kk][2][C], and the
+    // consumers read the interior knot values from X.
     // trace_rows > 0: trace is the base of a [trace_rows][K][2] array and the
     // row of this pass is st->trace_row (stop mode); otherwise trace points at
     // this pass's [K][2] block.
@@ -207,13 +211,16 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
     if (E > g.cap || E < 2) return;
     // Knot values of every channel (contiguous per knot), then the end-point
     // clamp of the two end knots (REF:447-486 max, 545-584 min).
-    real* y = yv + slot * (size_t)g.cap * g.C;
     const int C = g.C;
-    for (int idx = threadIdx.x; idx < E * C; idx += blockDim.x) {
-        const int i = idx / C, c = idx - i * C;
-        y[idx] = xval<real>(X[(size_t)kn[i] * C + c]);
+    real* y = yend ? yend + slot * 2 * (size_t)C : yv + slot * (size_t)g.cap * C;
+    const size_t last_row = yend ? (size_t)C : (size_t)(E - 1) * C;
+    if (!yend) {
+        for (int idx = threadIdx.x; idx < E * C; idx += blockDim.x) {
+            const int i = idx / C, c = idx - i * C;
+            y[idx] = xval<real>(X[(size_t)kn[i] * C + c]);
+        }
+        __syncthreads();  // the raw end values are written before the clamped ones replace them
     }
-    __syncthreads();  // the raw end values are written before the clamped ones replace them
     for (int c = threadIdx.x; c < C; c += blockDim.x) {
         real v0 = xval<real>(X[(size_t)kn[0] * C + c]);
         real vE = xval<real>(X[(size_t)kn[E - 1] * C + c]);
@@ -230,7 +237,7 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
             if (env == 0 ? (t > vE) : (t < vE)) vE = t;
         }
         y[c] = v0;
-        y[(size_t)(E - 1) * C + c] = vE;
+        y[last_row + c] = vE;
     }
 }
 
@@ -370,12 +377,15 @@ __device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, i
     return it;
 }
 
-template <typename real>
+template <typename real, typename XT>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
             real* __restrict__ dbuf, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
-            unsigned* __restrict__ bnd)
+            unsigned* __restrict__ bnd, const XT* __restrict__ X, const int* __restrict__ knots,
+            const real* __restrict__ yend)
 {
+    // X != nullptr: knot values read from the working signal, y_i = X[x_i]
+    // (interior knots) and yend (the clamped end knots), instead of yv
     constexpr int B = kSolveBatch;
     const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
     if (!it.ok) return;  // uniform over the warp
@@ -385,26 +395,44 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     const int cl = min(it.c, C - 1);
     const size_t slot = (size_t)it.env * Kc + it.kk;
     const Fac<real>* f = fac + slot * g.cap;
-    const real* y = yv + slot * (size_t)g.cap * C + cl;
+    const real* y = X ? nullptr : yv + slot * (size_t)g.cap * C + cl;
+    const int* kn = knots + slot * g.cap;
+    const real* ye = X ? yend + slot * 2 * (size_t)C + cl : nullptr;
+    // value of knot r at sample n (X mode)
+    auto yx = [&](int r, int n) -> real {
+        if (r == 0) return ye[0];
+        if (r == E - 1) return ye[C];
+        return xval<real>(X[(size_t)n * C + cl]);
+    };
     real* o = dbuf + slot * (size_t)g.cap * C + cl;
     const int is = (H < 0) ? 0 : max(0, i0 - H);
-    real yi = y[(size_t)is * C];
+    real yi = X ? yx(is, kn[is]) : y[(size_t)is * C];
     real slope_prev = real(0);
-    if (is > 0) slope_prev = mul_(sub_(yi, y[(size_t)(is - 1) * C]), f[is - 1].ih);
+    if (is > 0) slope_prev = mul_(sub_(yi, X ? yx(is - 1, kn[is - 1]) : y[(size_t)(is - 1) * C]), f[is - 1].ih);
     real dprev = real(0);
     float ymax = 0.0f;
     for (int base = is; base < i1; base += B) {
         const int nb = min(B, i1 - base);
         real fm = real(0), flm = real(0), fih = real(0);
+        int fx = 0;
         if (lane < nb) {
             const Fac<real> fr = f[base + lane];
             fm = fr.m;
             flm = fr.lm;
             fih = fr.ih;
+            if (X && base + 1 + lane < E) fx = kn[base + 1 + lane];
         }
         real yb[B];
+        if (X) {
 #pragma unroll
-        for (int k = 0; k < B; ++k) yb[k] = (k < nb && base + 1 + k < E) ? y[(size_t)(base + 1 + k) * C] : real(0);
+            for (int k = 0; k < B; ++k) {
+                const int n = __shfl_sync(0xffffffffu, fx, k);
+                yb[k] = (k < nb && base + 1 + k < E) ? yx(base + 1 + k, n) : real(0);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < B; ++k) yb[k] = (k < nb && base + 1 + k < E) ? y[(size_t)(base + 1 + k) * C] : real(0);
+        }
 #pragma unroll
         for (int k = 0; k < B; ++k) {
             const real m = shfl_idx_(fm, k), lm = shfl_idx_(flm, k), ih = shfl_idx_(fih, k);
@@ -974,10 +1002,11 @@ struct CumShared {
 
 template <int G>
 __global__ void __launch_bounds__(256, 3)
-k_mean_cum(float2* __restrict__ X, dd* __restrict__ acc_buf, const uint32_t* __restrict__ bits,
+k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restrict__ acc_buf,
+           const uint32_t* __restrict__ bits,
            const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
            const dd* __restrict__ rtab, const dd* __restrict__ rtab3, const dd* __restrict__ sv,
-           const dd* __restrict__ yv, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear,
+           const dd* __restrict__ yend, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear,
            const int* __restrict__ cumcfg, CumShared sh_g, Geom g, int k0, int Kc, int first_chunk, int last_chunk,
            RunState* st)
 {
@@ -1076,7 +1105,10 @@ k_mean_cum(float2* __restrict__ X, dd* __restrict__ acc_buf, const uint32_t* __r
             {
                 const int i = eI[le];
                 const int xi = eX[le], h = eH[le];
-                const dd y0 = yv[rb + (size_t)i * C], y1 = yv[rb + (size_t)(i + 1) * C];
+                // knot values: X at interior knots, the clamped ends (samples 0 and L - 1) from yend
+                const dd* ye = yend + slot * 2 * (size_t)C + cl;
+                const dd y0 = (xi == 0) ? ye[0] : xval<dd>(X[(size_t)xi * C + cl]);
+                const dd y1 = (xi + h == g.L - 1) ? ye[C] : xval<dd>(X[(size_t)(xi + h) * C + cl]);
                 const dd s0 = sv[rb + (size_t)i * C], s1 = sv[rb + (size_t)(i + 1) * C];
                 const dd d = (s1 - s0) * rtab3[h];
                 const dd s02(2.0f * s0.hi, 2.0f * s0.lo);  // exact
@@ -1261,7 +1293,7 @@ k_mean_cum(float2* __restrict__ X, dd* __restrict__ acc_buf, const uint32_t* __r
                 if (bad) tot = dd(__int_as_float(0x7fc00000), 0.0f);
                 const size_t off = (size_t)(p0 + r) * C + c;
                 if (!first_chunk) tot = tot + ac[k];
-                if (last_chunk) X[off] = xsub(xs[k], dd_mulf(tot, 0.5f) / qd);
+                if (last_chunk) Xout[off] = xsub(xs[k], dd_mulf(tot, 0.5f) / qd);
                 else acc_buf[off] = tot;
             }
         }

@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-epochs measurement")
     return ap.parse_args()
 
 
@@ -350,6 +351,13 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(y, outs["fp64"][1].cpu().numpy())
     if rank == 0 and not args.no_reference_gpu:
         line["reference_gpu"] = reference_gpu(y)
+    if not args.no_batched:
+        for p in plans.values():
+            p.close()
+        plans = {}
+        bres = batched_epochs(rank)
+        if rank == 0:
+            line["batched_epochs"] = bres
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -364,6 +372,65 @@ def run_ours(args):
 # algorithm) on a bounded sample: all 8 IMF stages with one sift each, scaled
 # to the 80 sifts of the full decomposition.
 # ----------------------------------------------------------------------------
+# batched epochs: 512 epochs of 32 channels, lengths uniform in [1024, 8192]
+# (seeded), 64 directions, 8 IMF slots x 10 sifts (fixed mode)
+BATCH = dict(workload="epochs512_c32_L1024-8192_k64_fixed", epochs=512, C=32, Lmin=1024, Lmax=8192, K=64,
+             num_imfs=8, max_iter=10, fs=256.0, warmup=1, steps=2)
+
+
+def batched_epochs(rank):
+    """Channel-samples/s of the batched mixed and FP64 paths on the epoch set,
+    with the per-IMF precision gate of the mixed form against FP64."""
+    import torch
+
+    import memd_gb300 as mg
+
+    B = BATCH
+    rng = np.random.default_rng(1000 + rank)
+    lengths = rng.integers(B["Lmin"], B["Lmax"] + 1, size=B["epochs"]).astype(np.int64)
+    C, K, NI, IT = B["C"], B["K"], B["num_imfs"], B["max_iter"]
+    recs = [mg.synth_eeg(C, int(L), B["fs"], seed=10_000 * (rank + 1) + e).astype(np.float32)
+            for e, L in enumerate(lengths)]
+    offs = np.concatenate([[0], np.cumsum(C * lengths)[:-1]]).astype(np.int64)
+    flat = np.concatenate([r.ravel() for r in recs])
+    d32 = mg.directions(C, K, dtype="f32")
+    out = {"workload": B["workload"], "epochs": int(B["epochs"]), "total_samples": int(lengths.sum()),
+           "channel_samples": int(C * lengths.sum())}
+    outs = {}
+    stream = torch.cuda.current_stream()
+    for name, prec, tdt in (("mixed", mg.PREC_MIXED, torch.float32), ("fp64", mg.PREC_F64, torch.float64)):
+        plan = mg.Plan(C, B["Lmax"], K, NI, IT, precision=prec, max_epochs=B["epochs"])
+        y = torch.as_tensor(flat, dtype=tdt, device="cuda")
+        o = torch.empty(NI * y.numel(), dtype=tdt, device="cuda")
+        d = d32.to(tdt)
+        for _ in range(B["warmup"]):
+            plan.run_batched(y, lengths, offs, d, o, stream=stream, stats=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(B["steps"]):
+            plan.run_batched(y, lengths, offs, d, o, stream=stream, stats=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / B["steps"]
+        st = plan.run_batched(y, lengths, offs, d, o)
+        out[name] = {"ms_per_step": ms, "channel_samples_per_s": C * float(lengths.sum()) / (ms / 1e3),
+                     "workspace_gb": plan.workspace_bytes / 1e9, "flags": int(st.flags)}
+        outs[name] = o.cpu().numpy().astype(np.float64)
+        plan.close()
+        del y, o
+        torch.cuda.empty_cache()
+    worst = 0.0
+    for off, L in zip(offs, lengths):
+        a = outs["mixed"][NI * off: NI * off + NI * C * L].reshape(NI, C, L)
+        b = outs["fp64"][NI * off: NI * off + NI * C * L].reshape(NI, C, L)
+        for i in range(NI):
+            worst = max(worst, rel_l2(a[i], b[i]))
+    out["precision_gate"] = {"max_rel_l2_per_imf_vs_fp64": worst, "passed": worst <= GATE}
+    out["mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    return out
+
+
 def cpu_baseline(y, dirs, reps: int = 1):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle

@@ -65,7 +65,7 @@ def _compile(src: str, extra_deps: list[str]) -> str:
     return obj
 
 
-EXAMPLES = ["sample_synthetic_signal", "memd_cli"]
+EXAMPLES = ["sample_synthetic_signal", "memd_cli", "memd_sweep"]
 BINDIR = os.path.join(PKG, "bin")
 MEX_STUB_DIR = os.path.join(REPO, "tests", "mex_stub")
 MEX_STUB_LIB = os.path.join(LIBDIR, "libmemd_mex_stub.so")

@@ -70,13 +70,22 @@ struct memd_plan {
     void* imf;
     void* yv;
     void* sv;
-    void* yend;  // impulse-accumulation mean: clamped end-knot values [2][Kc][2][C] (no yv gather)
+    void* yend;  // impulse-accumulation mean: clamped end-knot values [2][Kc][records][2][C] (no yv gather)
     void* dbuf;  // forward-eliminated right-hand sides [2][Kc][cap][C]
     void* fac;
     void* rtab;
     void* rtab3;  // impulse-accumulation mean: 1/(3h) as double-float
     unsigned* bnd;  // impulse-accumulation mean: [2 passes][2 parts][C] per-channel bounds (float bits)
     int* cumcfg;    // impulse-accumulation mean: anchor span (words) and CTAs per span, set by the factor kernel
+    // batched runs (cfg.max_epochs > 0): epochs concatenated at multiples of
+    // kEpochAlign samples; ep describes the current call's layout (n = 0: one record)
+    int batched;
+    int Lrec;                       // longest epoch (cfg.length)
+    memd::Epochs ep;
+    int* ep_dev;                    // off, len, cov [max_epochs] | w0 [max_epochs + 1] | wep [W capacity]
+    long long* ep_yoff;             // [max_epochs] caller offsets of the current call
+    std::vector<int64_t> ep_lens;   // lengths of the layout the graph was built for
+    std::vector<int> ep_host;       // staging of ep_dev
     memd::CumShared cumsh;  // impulse-accumulation mean: accumulators of spans split over CTAs
     void* M;     // stop mode: mean envelope of the last pass [L][C]
     void* part;  // stop mode: per channel group, direction and sample sum of (U-L)^2
@@ -166,7 +175,7 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
         dim3 grid((unsigned)((g.L + Sh::T - 1) / Sh::T), (unsigned)((g.C + G_ - 1) / G_));                 \
         k_eval<R, G_, S_><<<grid, 256, Sh::smem_bytes(p->Kc), s>>>(                                       \
             (R*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const Fac<R>*)p->fac,            \
-            (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part);      \
+            (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part, p->ep); \
         return;                                                                                            \
     }
         MEMD_EVAL_CASES(MEMD_CASE)
@@ -184,7 +193,7 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
             (const float2*)p->X, (float2*)p->Xb, (dd*)p->acc, p->bits, p->wpref, p->knots, p->cnt,               \
                                             (const dd*)p->rtab, (const dd*)p->rtab3, (const dd*)p->sv,           \
                                             (const dd*)p->yend, cur, other, p->cumcfg, p->cumsh, g, k0, kc, first,\
-                                            last, p->st);                                                          \
+                                            last, p->st, p->ep);                                                   \
         return;                                                                                                    \
     }
                 MEMD_CASE(32) MEMD_CASE(16) MEMD_CASE(8)
@@ -273,21 +282,23 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.begin();
         if constexpr (P == MEMD_PREC_MIXED)
             k_project_mx<<<pg, 256, p->proj_smem, s>>>((const float2*)p->X, (const float*)p->dir,
-                                                       (const float*)p->dir + (size_t)g.K * g.C, p->bits, g, k0, kc, p->st);
+                                                       (const float*)p->dir + (size_t)g.K * g.C, p->bits, g, k0, kc, p->st,
+                                                       p->ep);
         else
-            k_project_extrema<R, XT><<<pg, 256, p->proj_smem, s>>>((const XT*)p->X, (const R*)p->dir, p->bits, g, k0, kc);
+            k_project_extrema<R, XT><<<pg, 256, p->proj_smem, s>>>((const XT*)p->X, (const R*)p->dir, p->bits, g, k0, kc,
+                                                                   p->ep);
         lc.end(MEMD_STAGE_PROJECT);
         lc.begin();
         k_compact<R, XT><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (R*)p->yv,
                                                             (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows,
-                                                            p->cum ? (R*)p->yend : nullptr);
+                                                            p->cum ? (R*)p->yend : nullptr, p->ep);
         lc.end(MEMD_STAGE_COMPACT);
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
         lc.begin();
         k_factor<R><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
                                                                  (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
-                                                                 p->cum ? p->cumcfg : nullptr);
+                                                                 p->cum ? p->cumcfg : nullptr, p->ep);
         lc.end(MEMD_STAGE_FACTOR);
         const long nseg = (p->H < 0) ? 1 : (g.cap + p->Ss - 1) / p->Ss;
         const long ns = 2L * kc * nseg * p->ngroups * 32;
@@ -297,7 +308,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         k_solve_fwd<R, XT><<<nb, kSolveThreads, 0, s>>>((const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g,
                                                        k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
                                                        p->cum ? (const XT*)p->X : nullptr, p->knots,
-                                                       p->cum ? (const R*)p->yend : nullptr);
+                                                       p->cum ? (const R*)p->yend : nullptr, p->ep);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         k_solve_bwd<R><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0,
@@ -553,6 +564,110 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Pre
     return MEMD_OK;
 }
 
+// Batched run: lay the epochs out at multiples of kEpochAlign samples (the
+// graph is rebuilt when the set of lengths changes), scatter the records into
+// the working signal, run the decomposition graph over all of them at once,
+// and scatter the IMFs back to each epoch's block.
+template <int P>
+static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths, const int64_t* offsets,
+                                    const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
+                                    typename Prec<P>::T* d_imfs, void* stream, memd_stats* stats)
+{
+    using XT = typename Prec<P>::X;
+    using T = typename Prec<P>::T;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!p->batched) return set_error(MEMD_ERR_UNSUPPORTED, "run_batched: the plan was created without max_epochs");
+    if (n < 1 || n > p->cfg.max_epochs) return set_error(MEMD_ERR_INVALID, "run_batched: n_epochs out of range");
+    if (!lengths || !offsets || !d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run_batched: null argument");
+    for (int e = 0; e < n; ++e) {
+        if (lengths[e] < 4 || lengths[e] > p->Lrec) return set_error(MEMD_ERR_INVALID, "run_batched: epoch length out of range");
+        if (offsets[e] < 0) return set_error(MEMD_ERR_INVALID, "run_batched: negative offset");
+    }
+    const int C = p->g.C;
+    cudaError_t e;
+    std::vector<int64_t> lens(lengths, lengths + n);
+    if (lens != p->ep_lens || !p->exec) {
+        // layout: off[e] = sum of the earlier lengths rounded up to kEpochAlign
+        const int me = (int)p->cfg.max_epochs;
+        std::vector<int> off(n), cov(n), w0(n + 1);
+        int64_t acc = 0;
+        for (int i = 0; i < n; ++i) {
+            off[i] = (int)acc;
+            const int Le = (int)lens[i];
+            cov[i] = p->cfg.ref_window ? 240 * ((Le + 241) / 242) : Le;
+            w0[i] = (int)(acc / 32);
+            acc += (Le + kEpochAlign - 1) / kEpochAlign * kEpochAlign;
+        }
+        const int Ltot = (int)acc, W = Ltot / 32;
+        w0[n] = W;
+        p->ep_host.assign(4 * (size_t)me + 1 + (size_t)W, 0);
+        int* h = p->ep_host.data();
+        for (int i = 0; i < n; ++i) {
+            h[i] = off[i];
+            h[me + i] = (int)lens[i];
+            h[2 * me + i] = cov[i];
+        }
+        for (int i = 0; i <= n; ++i) h[3 * me + i] = w0[i];
+        int* wep = h + 4 * me + 1;
+        for (int i = 0; i < n; ++i)
+            for (int w = w0[i]; w < w0[i + 1]; ++w) wep[w] = i;
+        e = cudaMemcpy(p->ep_dev, h, sizeof(int) * p->ep_host.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return set_cuda_error("run_batched: epoch table", e);
+        p->ep.n = n;
+        p->ep.off = p->ep_dev;
+        p->ep.len = p->ep_dev + me;
+        p->ep.cov = p->ep_dev + 2 * me;
+        p->ep.w0 = p->ep_dev + 3 * me;
+        p->ep.wep = p->ep_dev + 4 * me + 1;
+        p->g.L = Ltot;
+        p->g.W = W;
+        if (p->exec) cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+        p->ep_lens = lens;
+    }
+    const Geom& g = p->g;
+    const size_t CL = (size_t)C * g.L;
+    std::vector<long long> yoff(offsets, offsets + n);
+    e = cudaMemcpyAsync(p->ep_yoff, yoff.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return set_cuda_error("run_batched: offsets", e);
+    memd_status st = build_graph<P>(p);
+    if (st != MEMD_OK) return st;
+    cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
+    // the gaps between epochs stay zero in every working buffer
+    cudaMemsetAsync(p->run, 0, CL * sizeof(XT), s);
+    cudaMemsetAsync(p->X, 0, CL * sizeof(XT), s);
+    if (p->Xb) cudaMemsetAsync(p->Xb, 0, CL * sizeof(XT), s);
+    k_batched_in<XT, T><<<dim3((unsigned)g.W, (unsigned)((C + 31) / 32)), dim3(32, 8), 0, s>>>(d_y, p->ep_yoff, (XT*)p->run,
+                                                                                              C, p->ep);
+    cudaMemcpyAsync(p->dir, d_dir, sizeof(T) * (size_t)g.K * C, cudaMemcpyDeviceToDevice, s);
+    if constexpr (P == MEMD_PREC_MIXED)
+        cudaMemsetAsync((float*)p->dir + (size_t)g.K * C, 0, sizeof(float) * (size_t)g.K * C, s);
+    cudaEventRecord(p->e0, s);
+    e = cudaGraphLaunch(p->exec, s);
+    if (e != cudaSuccess) return set_cuda_error("run_batched: graph launch", e);
+    cudaEventRecord(p->e1, s);
+    k_batched_out<T><<<1024, 256, 0, s>>>((const T*)p->imf, p->ep_yoff, d_imfs, C, g.L, (int)p->cfg.num_imfs, p->ep);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error("run_batched: launch", e);
+    if (stats) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return set_cuda_error("run_batched: synchronize", e);
+        RunState hs;
+        e = cudaMemcpy(&hs, p->st, sizeof(RunState), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return set_cuda_error("run_batched: read state", e);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->e0, p->e1);
+        memset(stats, 0, sizeof(*stats));
+        stats->elapsed_ms = ms;
+        stats->flags = hs.flags;
+        stats->n_imfs = (int)p->cfg.num_imfs - 1;
+        stats->launches = p->graph_launches + 2;
+        for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
+        stats->refined = hs.pad[3];
+    }
+    return MEMD_OK;
+}
+
 template <int P>
 static memd_status profile_impl(memd_plan* p, const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
                                 typename Prec<P>::T* d_imfs, void* stream, memd_profile* prof)
@@ -663,9 +778,26 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         return set_error(MEMD_ERR_INVALID, "plan: bad stop mode");
     if (c.stop_mode == MEMD_STOP_CRITERION && (c.max_iter < 1 || !(c.stop_sd > 0) || !(c.stop_sd2 > 0) || c.stop_tol < 0))
         return set_error(MEMD_ERR_INVALID, "plan: stop criterion needs max_iter >= 1 and positive thresholds");
+    if (c.max_epochs < 0 || c.max_epochs > (1 << 20)) return set_error(MEMD_ERR_INVALID, "plan: bad max_epochs");
+    if (c.max_epochs > 0) {
+        if (c.precision == MEMD_PREC_F32)
+            return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the FP64 and mixed forms");
+        if (c.stop_mode != MEMD_STOP_FIXED)
+            return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the fixed mode");
+        if (c.precision == MEMD_PREC_MIXED && c.mean_eval == 1)
+            return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched mixed runs use the impulse-accumulation mean");
+        if ((int64_t)c.max_epochs * ((c.length + kEpochAlign - 1) / kEpochAlign * kEpochAlign) > (1LL << 28))
+            return set_error(MEMD_ERR_INVALID, "plan: max_epochs x length exceeds 2^28 samples");
+    }
     memd_plan* p = new memd_plan();  // value-initialised: every pointer and count starts at zero
     p->cfg = c;
-    const int C = (int)c.channels, L = (int)c.length, K = (int)c.directions;
+    const int C = (int)c.channels, K = (int)c.directions;
+    p->batched = c.max_epochs > 0;
+    p->Lrec = (int)c.length;
+    // batched: room for max_epochs epochs of the longest length, each padded to
+    // a multiple of kEpochAlign samples
+    const int L = p->batched ? (int)(c.max_epochs * ((c.length + kEpochAlign - 1) / kEpochAlign * kEpochAlign))
+                             : (int)c.length;
     p->prec = c.precision;
     const bool f64 = c.precision == MEMD_PREC_F64;
     p->real_bytes = (f64 || c.precision == MEMD_PREC_MIXED) ? 8 : 4;  // double, float or double-float
@@ -675,9 +807,14 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     p->g.L = L;
     p->g.K = K;
     p->g.W = (L + 31) / 32;
-    p->g.cap = (L + 1) / 2 + 4;
+    p->g.cap = p->batched ? L / 2 + 5 * (int)c.max_epochs + 4 : (L + 1) / 2 + 4;
     p->g.cov = c.ref_window ? 240 * ((L + 241) / 242) : L;
     p->Kc = (c.dir_chunk > 0) ? std::min<int>((int)c.dir_chunk, K) : K;
+    if (p->batched && c.dir_chunk <= 0) {
+        // keep each [2][Kc][cap][C] knot array under ~16 GB
+        const double per_dir = 2.0 * 8.0 * (double)p->g.cap * C;
+        p->Kc = (int)std::max(1.0, std::min((double)K, std::floor(16e9 / per_dir)));
+    }
     p->Kc = std::min(p->Kc, 1024);
     p->nchunks = (K + p->Kc - 1) / p->Kc;
     if (c.solve_window < 0) {
@@ -762,12 +899,13 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     ALLOC(p->cnt, sizeof(int) * 2 * (size_t)K);
     ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
     if (!p->cum) ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
-    else ALLOC(p->yend, rb * 2 * Kc * 2 * C);
+    else ALLOC(p->yend, rb * 2 * Kc * (size_t)std::max<int64_t>(1, c.max_epochs) * 2 * C);  // [2][Kc][epochs][2][C]
     ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->dbuf, rb * 2 * Kc * p->g.cap * C);
-    ALLOC(p->rtab, rb * (size_t)(L + 1));
+    const int Lh = p->batched ? std::max(p->Lrec, kEpochAlign) : L;  // longest knot gap
+    ALLOC(p->rtab, rb * (size_t)(Lh + 1));
     if (p->cum) {
-        ALLOC(p->rtab3, sizeof(dd) * (size_t)(L + 1));
+        ALLOC(p->rtab3, sizeof(dd) * (size_t)(Lh + 1));
         ALLOC(p->bnd, sizeof(unsigned) * 4 * (size_t)C);
         ALLOC(p->cumcfg, sizeof(int) * 4);
         ALLOC(p->cumsh.kq, sizeof(unsigned long long) * 35 * (size_t)p->g.W * C);
@@ -778,6 +916,12 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         ALLOC(p->M, rb * CL);
         ALLOC(p->part, rb * (size_t)p->egroups * Kc * L);
         ALLOC(p->amp, rb * (size_t)L);
+    }
+    if (p->batched) {
+        const size_t me = (size_t)c.max_epochs;
+        ALLOC(p->ep_dev, sizeof(int) * (4 * me + 1 + (size_t)p->g.W));
+        ALLOC(p->ep_yoff, sizeof(long long) * me);
+        ALLOC(p->ep.cnt, sizeof(int) * 2 * (size_t)K * me);
     }
     ALLOC(p->st, sizeof(RunState));
     ALLOC(p->coord_bad, sizeof(int));
@@ -800,13 +944,13 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         double* r64 = nullptr;
         float* r32 = nullptr;
         dd* rdd = nullptr;
-        e = cudaMalloc((void**)&r64, sizeof(double) * (size_t)(L + 1));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&r32, sizeof(float) * (size_t)(L + 1));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&rdd, sizeof(dd) * (size_t)(L + 1));
+        e = cudaMalloc((void**)&r64, sizeof(double) * (size_t)(Lh + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&r32, sizeof(float) * (size_t)(Lh + 1));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&rdd, sizeof(dd) * (size_t)(Lh + 1));
         if (e == cudaSuccess) {
-            k_fill_reciprocals<<<256, 256>>>(r64, r32, rdd, (dd*)p->rtab3, L + 1);
+            k_fill_reciprocals<<<256, 256>>>(r64, r32, rdd, (dd*)p->rtab3, Lh + 1);
             const void* src = f64 ? (void*)r64 : (c.precision == MEMD_PREC_MIXED ? (void*)rdd : (void*)r32);
-            e = cudaMemcpy(p->rtab, src, rb * (size_t)(L + 1), cudaMemcpyDeviceToDevice);
+            e = cudaMemcpy(p->rtab, src, rb * (size_t)(Lh + 1), cudaMemcpyDeviceToDevice);
         }
         cudaFree(r64);
         cudaFree(r32);
@@ -856,6 +1000,7 @@ memd_status memd_run_f64(memd_plan* plan, const int32_t* d_x, const double* d_y,
     if (!plan) return set_error(MEMD_ERR_INVALID, "run: null plan");
     if (!d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run: null pointer");
     if (plan->prec != MEMD_PREC_F64) return set_error(MEMD_ERR_PRECISION, "run_f64: plan is not FP64");
+    if (plan->batched) return set_error(MEMD_ERR_UNSUPPORTED, "run_f64: batched plan: use memd_run_batched_f64");
     return run_impl<MEMD_PREC_F64>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
 }
 
@@ -865,6 +1010,7 @@ memd_status memd_run_f32(memd_plan* plan, const int32_t* d_x, const float* d_y, 
     using namespace memd;
     if (!plan) return set_error(MEMD_ERR_INVALID, "run: null plan");
     if (!d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run: null pointer");
+    if (plan->batched) return set_error(MEMD_ERR_UNSUPPORTED, "run_f32: batched plan: use memd_run_batched_f32");
     if (plan->prec == MEMD_PREC_F32) return run_impl<MEMD_PREC_F32>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
     if (plan->prec == MEMD_PREC_MIXED) return run_impl<MEMD_PREC_MIXED>(plan, d_x, d_y, d_dir, d_imfs, stream, stats);
     return set_error(MEMD_ERR_PRECISION, "run_f32: plan is FP64");
@@ -876,6 +1022,7 @@ memd_status memd_profile_f64(memd_plan* plan, const double* d_y, const double* d
     using namespace memd;
     if (!plan || !d_y || !d_dir || !d_imfs || !prof) return set_error(MEMD_ERR_INVALID, "profile: null argument");
     if (plan->prec != MEMD_PREC_F64) return set_error(MEMD_ERR_PRECISION, "profile_f64: plan is not FP64");
+    if (plan->batched) return set_error(MEMD_ERR_UNSUPPORTED, "profile: batched plans are not profiled");
     return profile_impl<MEMD_PREC_F64>(plan, d_y, d_dir, d_imfs, stream, prof);
 }
 
@@ -884,21 +1031,30 @@ memd_status memd_profile_f32(memd_plan* plan, const float* d_y, const float* d_d
 {
     using namespace memd;
     if (!plan || !d_y || !d_dir || !d_imfs || !prof) return set_error(MEMD_ERR_INVALID, "profile: null argument");
+    if (plan->batched) return set_error(MEMD_ERR_UNSUPPORTED, "profile: batched plans are not profiled");
     if (plan->prec == MEMD_PREC_F32) return profile_impl<MEMD_PREC_F32>(plan, d_y, d_dir, d_imfs, stream, prof);
     if (plan->prec == MEMD_PREC_MIXED) return profile_impl<MEMD_PREC_MIXED>(plan, d_y, d_dir, d_imfs, stream, prof);
     return set_error(MEMD_ERR_PRECISION, "profile_f32: plan is FP64");
 }
 
-memd_status memd_run_batched_f64(memd_plan*, int32_t, const int64_t*, const int64_t*, const double*,
-                                 const double*, double*, void*, memd_stats*)
+memd_status memd_run_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths, const int64_t* offsets,
+                                 const double* d_y, const double* d_dir, double* d_imfs, void* stream, memd_stats* stats)
 {
-    return memd::set_error(MEMD_ERR_UNSUPPORTED, "batched runs are not built in this library");
+    using namespace memd;
+    if (!plan) return set_error(MEMD_ERR_INVALID, "run_batched: null plan");
+    if (plan->prec != MEMD_PREC_F64) return set_error(MEMD_ERR_PRECISION, "run_batched_f64: plan is not FP64");
+    return run_batched_impl<MEMD_PREC_F64>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream, stats);
 }
 
-memd_status memd_run_batched_f32(memd_plan*, int32_t, const int64_t*, const int64_t*, const float*,
-                                 const float*, float*, void*, memd_stats*)
+memd_status memd_run_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_t* lengths, const int64_t* offsets,
+                                 const float* d_y, const float* d_dir, float* d_imfs, void* stream, memd_stats* stats)
 {
-    return memd::set_error(MEMD_ERR_UNSUPPORTED, "batched runs are not built in this library");
+    using namespace memd;
+    if (!plan) return set_error(MEMD_ERR_INVALID, "run_batched: null plan");
+    if (plan->prec == MEMD_PREC_MIXED)
+        return run_batched_impl<MEMD_PREC_MIXED>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream, stats);
+    if (plan->prec == MEMD_PREC_F32) return set_error(MEMD_ERR_UNSUPPORTED, "run_batched_f32: FP32 plans are not batched");
+    return set_error(MEMD_ERR_PRECISION, "run_batched_f32: plan is FP64");
 }
 
 }  // extern "C"

@@ -151,6 +151,60 @@ struct Geom {
     int cov;    // last interior sample tested for extrema
 };
 
+// Batched runs: the epochs are concatenated along the sample axis, each
+// starting at a multiple of kEpochAlign samples (so that no 32-sample word,
+// evaluation tile or anchor span holds samples of two epochs; the gap samples
+// are zero and never tested, fitted or written).  n == 0: a single record
+// described by Geom alone.
+constexpr int kEpochAlign = 512;
+struct Epochs {
+    int n;
+    const int* off;  // [n] first sample of epoch e in the concatenated record
+    const int* len;  // [n] its length
+    const int* cov;  // [n] last interior sample tested for extrema (epoch-local index)
+    const int* w0;   // [n + 1] first word of epoch e; w0[n] = W
+    const int* wep;  // [W] epoch of each word
+    int* cnt;        // [2][K][n] knots per (envelope, direction, epoch)
+};
+
+// Extremum rule of sample n: inside the record, a forced end point (first or
+// last sample of its record), or an interior sample that is tested.
+__device__ __forceinline__ void sample_rule(const Geom& g, const Epochs& ep, int n, bool& inrange, bool& endpt,
+                                            bool& interior)
+{
+    if (ep.n == 0) {
+        inrange = n < g.L;
+        endpt = (n == 0) || (n == g.L - 1);
+        interior = (n >= 1) && (n <= min(g.cov, g.L - 2));
+        return;
+    }
+    if (n >= g.L) {
+        inrange = endpt = interior = false;
+        return;
+    }
+    const int e = ep.wep[n >> 5];
+    const int t = n - ep.off[e], Le = ep.len[e];
+    inrange = t < Le;
+    endpt = (t == 0) || (t == Le - 1);
+    interior = (t >= 1) && (t <= min(ep.cov[e], Le - 2));
+}
+
+// Is knot i (at sample x, of E knots) the first or last knot of its record?
+__device__ __forceinline__ bool record_end_knot(const Epochs& ep, int x, int i, int E)
+{
+    if (ep.n == 0) return i == 0 || i == E - 1;
+    const int e = ep.wep[x >> 5];
+    const int o = ep.off[e];
+    return x == o || x == o + ep.len[e] - 1;
+}
+
+// Do both envelopes of direction k have more than 3 knots in epoch e?
+__device__ __forceinline__ bool dir_qualifies(const Geom& g, const Epochs& ep, const int* cnt, int k, int e)
+{
+    if (ep.n == 0) return cnt[k] > 3 && cnt[g.K + k] > 3;
+    return ep.cnt[(size_t)k * ep.n + e] > 3 && ep.cnt[((size_t)g.K + k) * ep.n + e] > 3;
+}
+
 // Per-run device state (counters and sticky flags).
 struct RunState {
     int flags;                 // MEMD_FLAG_* bits
@@ -220,6 +274,9 @@ __device__ __forceinline__ dd sqrt_(dd a) { return dd_sqrt(a); }
 __device__ __forceinline__ double fmat_(double a, float t, double c) { return __fma_rn(a, (double)t, c); }
 __device__ __forceinline__ float fmat_(float a, float t, float c) { return __fmaf_rn(a, t, c); }
 __device__ __forceinline__ dd fmat_(dd a, float t, dd c) { return dd_mulf(a, t) + c; }
+__device__ __forceinline__ bool is_zero(double v) { return v == 0.0; }
+__device__ __forceinline__ bool is_zero(float v) { return v == 0.0f; }
+__device__ __forceinline__ bool is_zero(dd v) { return v.hi == 0.0f; }
 // magnitude as a float (bounds only: the float may round down by 1 ulp)
 __device__ __forceinline__ float magf(double v) { return (float)fabs(v); }
 __device__ __forceinline__ float magf(float v) { return fabsf(v); }

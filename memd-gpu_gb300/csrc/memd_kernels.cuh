@@ -53,7 +53,7 @@ constexpr int kProjTK = 16;
 template <typename real, typename XT>
 __global__ void __launch_bounds__(256)
 k_project_extrema(const XT* __restrict__ X, const real* __restrict__ dir,
-                  uint32_t* __restrict__ bits, Geom g, int k0, int Kc)
+                  uint32_t* __restrict__ bits, Geom g, int k0, int Kc, Epochs ep)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int C = g.C;
@@ -101,10 +101,8 @@ k_project_extrema(const XT* __restrict__ X, const real* __restrict__ dir,
     __syncthreads();
     const int n = n0 + sg * 32 + lane;
     const int r = 1 + sg * 32 + lane;
-    const int last = min(g.cov, g.L - 2);
-    const bool inrange = n < g.L;
-    const bool endpt = (n == 0) || (n == g.L - 1);
-    const bool interior = (n >= 1) && (n <= last);
+    bool inrange, endpt, interior;
+    sample_rule(g, ep, n, inrange, endpt, interior);
     const int w = (n0 >> 5) + sg;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -130,7 +128,7 @@ __global__ void __launch_bounds__(512)
 k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __restrict__ knots,
           int* __restrict__ cnt, real* __restrict__ yv, const XT* __restrict__ X,
           memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st, int trace_rows,
-          real* __restrict__ yend)
+          real* __restrict__ yend, Epochs ep)
 {
     // yend != nullptr: the knot values are not gathered; only the two end
     // knots' values (clamped) are written, to yend[env][kk][2][C], and the
@@ -210,34 +208,50 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
     }
     if (E > g.cap || E < 2) return;
     // Knot values of every channel (contiguous per knot), then the end-point
-    // clamp of the two end knots (REF:447-486 max, 545-584 min).
+    // clamp of the two end knots of each record (REF:447-486 max, 545-584 min).
     const int C = g.C;
-    real* y = yend ? yend + slot * 2 * (size_t)C : yv + slot * (size_t)g.cap * C;
-    const size_t last_row = yend ? (size_t)C : (size_t)(E - 1) * C;
+    const int nrec = ep.n > 0 ? ep.n : 1;
+    if (ep.n > 0) {
+        for (int e = threadIdx.x; e < ep.n; e += blockDim.x)
+            ep.cnt[((size_t)env * g.K + k0 + kk) * ep.n + e] = wp[ep.w0[e + 1]] - wp[ep.w0[e]];
+    }
     if (!yend) {
+        real* y = yv + slot * (size_t)g.cap * C;
         for (int idx = threadIdx.x; idx < E * C; idx += blockDim.x) {
             const int i = idx / C, c = idx - i * C;
             y[idx] = xval<real>(X[(size_t)kn[i] * C + c]);
         }
         __syncthreads();  // the raw end values are written before the clamped ones replace them
     }
-    for (int c = threadIdx.x; c < C; c += blockDim.x) {
-        real v0 = xval<real>(X[(size_t)kn[0] * C + c]);
-        real vE = xval<real>(X[(size_t)kn[E - 1] * C + c]);
-        if (E - 1 > 4) {
-            const real v1 = xval<real>(X[(size_t)kn[1] * C + c]);
-            const real v2 = xval<real>(X[(size_t)kn[2] * C + c]);
-            real slope = div_(sub_(v2, v1), real(kn[2] - kn[1]));
-            real t = fmad_(-slope, real(kn[1] - kn[0]), v1);
+    for (int idx = threadIdx.x; idx < nrec * C; idx += blockDim.x) {
+        const int e = idx / C, c = idx - e * C;
+        const int kb = ep.n > 0 ? wp[ep.w0[e]] : 0;
+        const int ke = ep.n > 0 ? wp[ep.w0[e + 1]] : E;  // the record's knots: kb .. ke - 1
+        const int Er = ke - kb;
+        const int* kr = kn + kb;
+        real v0 = xval<real>(X[(size_t)kr[0] * C + c]);
+        real vE = xval<real>(X[(size_t)kr[Er - 1] * C + c]);
+        if (Er - 1 > 4) {
+            const real v1 = xval<real>(X[(size_t)kr[1] * C + c]);
+            const real v2 = xval<real>(X[(size_t)kr[2] * C + c]);
+            real slope = div_(sub_(v2, v1), real(kr[2] - kr[1]));
+            real t = fmad_(-slope, real(kr[1] - kr[0]), v1);
             if (env == 0 ? (t > v0) : (t < v0)) v0 = t;
-            const real a = xval<real>(X[(size_t)kn[E - 3] * C + c]);
-            const real bb = xval<real>(X[(size_t)kn[E - 2] * C + c]);
-            slope = div_(sub_(bb, a), real(kn[E - 2] - kn[E - 3]));
-            t = fmad_(slope, real(kn[E - 1] - kn[E - 2]), bb);
+            const real a = xval<real>(X[(size_t)kr[Er - 3] * C + c]);
+            const real bb = xval<real>(X[(size_t)kr[Er - 2] * C + c]);
+            slope = div_(sub_(bb, a), real(kr[Er - 2] - kr[Er - 3]));
+            t = fmad_(slope, real(kr[Er - 1] - kr[Er - 2]), bb);
             if (env == 0 ? (t > vE) : (t < vE)) vE = t;
         }
-        y[c] = v0;
-        y[last_row + c] = vE;
+        if (yend) {
+            real* ye = yend + ((slot * nrec) + e) * 2 * (size_t)C;
+            ye[c] = v0;
+            ye[C + c] = vE;
+        } else {
+            real* y = yv + slot * (size_t)g.cap * C;
+            y[(size_t)kb * C + c] = v0;
+            y[(size_t)(ke - 1) * C + c] = vE;
+        }
     }
 }
 
@@ -250,7 +264,8 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
 template <typename real>
 __global__ void __launch_bounds__(128)
 k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real* __restrict__ rtab,
-         Fac<real>* __restrict__ fac, Geom g, int k0, int Kc, int Sf, int Hf, int* __restrict__ cumcfg)
+         Fac<real>* __restrict__ fac, Geom g, int k0, int Kc, int Sf, int Hf, int* __restrict__ cumcfg,
+         Epochs ep)
 {
     // cumcfg != nullptr (impulse-accumulation mean): block 0 picks the mean
     // kernel's anchor span, 32 m samples (m the largest power of two <= 8 with
@@ -300,7 +315,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
     for (int i = js; i < i1; ++i) {
         const int xr = (i < E - 1) ? x[i + 1] : xi;
         real l, d, u;
-        if (i == 0 || i == E - 1) {
+        if (record_end_knot(ep, xi, i, E)) {  // natural end conditions: s = 0
             l = real(0); d = real(1); u = real(0);
         } else {
             const int hl = xi - xl, hr = xr - xi;
@@ -382,10 +397,12 @@ __global__ void __launch_bounds__(kSolveThreads)
 k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
             real* __restrict__ dbuf, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
             unsigned* __restrict__ bnd, const XT* __restrict__ X, const int* __restrict__ knots,
-            const real* __restrict__ yend)
+            const real* __restrict__ yend, Epochs ep)
 {
     // X != nullptr: knot values read from the working signal, y_i = X[x_i]
-    // (interior knots) and yend (the clamped end knots), instead of yv
+    // (interior knots) and yend (the clamped end knots of each record),
+    // instead of yv.  Rows of a record's end knots are the identity rows of
+    // the factorisation (lm == 0): their right-hand side is 0.
     constexpr int B = kSolveBatch;
     const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
     if (!it.ok) return;  // uniform over the warp
@@ -397,37 +414,59 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     const Fac<real>* f = fac + slot * g.cap;
     const real* y = X ? nullptr : yv + slot * (size_t)g.cap * C + cl;
     const int* kn = knots + slot * g.cap;
-    const real* ye = X ? yend + slot * 2 * (size_t)C + cl : nullptr;
-    // value of knot r at sample n (X mode)
-    auto yx = [&](int r, int n) -> real {
-        if (r == 0) return ye[0];
-        if (r == E - 1) return ye[C];
+    const int nrec = ep.n > 0 ? ep.n : 1;
+    const real* ye = X ? yend + slot * nrec * 2 * (size_t)C + cl : nullptr;
+    // (X mode) knot r at sample n: its record and whether it is the record's
+    // first (1) or last (2) knot
+    auto endfl = [&](int r, int n, int& e) -> int {
+        if (ep.n == 0) {
+            e = 0;
+            return r == 0 ? 1 : (r == E - 1 ? 2 : 0);
+        }
+        e = ep.wep[n >> 5];
+        const int o = ep.off[e];
+        return n == o ? 1 : (n == o + ep.len[e] - 1 ? 2 : 0);
+    };
+    auto yx = [&](int n, int fl, int e) -> real {
+        if (fl) return ye[(size_t)e * 2 * C + (fl == 2 ? C : 0)];
         return xval<real>(X[(size_t)n * C + cl]);
+    };
+    auto yrow = [&](int r) -> real {
+        if (!X) return y[(size_t)r * C];
+        const int n = kn[r];
+        int e;
+        const int fl = endfl(r, n, e);
+        return yx(n, fl, e);
     };
     real* o = dbuf + slot * (size_t)g.cap * C + cl;
     const int is = (H < 0) ? 0 : max(0, i0 - H);
-    real yi = X ? yx(is, kn[is]) : y[(size_t)is * C];
+    real yi = yrow(is);
     real slope_prev = real(0);
-    if (is > 0) slope_prev = mul_(sub_(yi, X ? yx(is - 1, kn[is - 1]) : y[(size_t)(is - 1) * C]), f[is - 1].ih);
+    if (is > 0) slope_prev = mul_(sub_(yi, yrow(is - 1)), f[is - 1].ih);
     real dprev = real(0);
     float ymax = 0.0f;
     for (int base = is; base < i1; base += B) {
         const int nb = min(B, i1 - base);
         real fm = real(0), flm = real(0), fih = real(0);
-        int fx = 0;
+        int fx = 0, ffl = 0, fe = 0;
         if (lane < nb) {
             const Fac<real> fr = f[base + lane];
             fm = fr.m;
             flm = fr.lm;
             fih = fr.ih;
-            if (X && base + 1 + lane < E) fx = kn[base + 1 + lane];
+            if (X && base + 1 + lane < E) {
+                fx = kn[base + 1 + lane];
+                ffl = endfl(base + 1 + lane, fx, fe);
+            }
         }
         real yb[B];
         if (X) {
 #pragma unroll
             for (int k = 0; k < B; ++k) {
                 const int n = __shfl_sync(0xffffffffu, fx, k);
-                yb[k] = (k < nb && base + 1 + k < E) ? yx(base + 1 + k, n) : real(0);
+                const int fl = __shfl_sync(0xffffffffu, ffl, k);
+                const int e = __shfl_sync(0xffffffffu, fe, k);
+                yb[k] = (k < nb && base + 1 + k < E) ? yx(n, fl, e) : real(0);
             }
         } else {
 #pragma unroll
@@ -441,7 +480,7 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 const real ynext = yb[k];
                 real slope = real(0), r = real(0);
                 if (i < E - 1) slope = mul_(sub_(ynext, yi), ih);
-                if (i > 0 && i < E - 1) r = mul_(real(3), sub_(slope, slope_prev));
+                if (!is_zero(lm)) r = mul_(real(3), sub_(slope, slope_prev));
                 const real dcur = fmad_(-lm, dprev, mul_(m, r));
                 // rows before i0 only warm the recurrence up
                 if (i >= i0) {
@@ -531,7 +570,7 @@ struct EvalShape {
     static constexpr int MI = T / 2 + 4;
     static size_t smem_bytes(int Kc)
     {
-        return sizeof(real) * ((size_t)MI * 4 * G + T + MI) + sizeof(int) * ((size_t)(MI + 1) + T + T / 32 + 6 * Kc + 4);
+        return sizeof(real) * ((size_t)MI * 4 * G + T + MI) + sizeof(int) * ((size_t)(MI + 1) + T + T / 32 + 8 * Kc + 4);
     }
 };
 
@@ -541,7 +580,7 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
        const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
        const Fac<real>* __restrict__ fac, const real* __restrict__ sv, const real* __restrict__ yv, Geom g,
        int k0, int Kc, int first_chunk, int last_chunk, RunState* st, real* __restrict__ M,
-       real* __restrict__ part)
+       real* __restrict__ part, Epochs ep)
 {
     // M == nullptr: fixed mode, the last chunk updates X in place.
     // M != nullptr: stop mode, the last chunk writes the mean envelope to M and
@@ -557,7 +596,7 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
     int* kx = reinterpret_cast<int*>(ihs + MI);       // [MI + 1]
     int* lis = kx + MI + 1;                           // [T]
     uint32_t* wds = reinterpret_cast<uint32_t*>(lis + T);  // [T/32]
-    int* tab = reinterpret_cast<int*>(wds + T / 32);  // [2*Kc][3]
+    int* tab = reinterpret_cast<int*>(wds + T / 32);  // [2*Kc][3]; batched: + [1] + [2*Kc] record knot bases
     int* sQ = tab + 6 * Kc;
 
     const int n0 = blockIdx.x * T;
@@ -566,7 +605,11 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
     const int row = threadIdx.x / G;
     const int c = cg * G + cc;
     const bool cok = c < g.C;
-    const int nl = min(T, g.L - n0);
+    // the tile's record (epoch): tiles (T | 512) never straddle two
+    const int rec = ep.n > 0 ? ep.wep[n0 >> 5] : 0;
+    const int rend = ep.n > 0 ? ep.off[rec] + ep.len[rec] : g.L;
+    if (n0 >= rend) return;  // gap between epochs; uniform over the CTA
+    const int nl = min(T, rend - n0);
     const int C = g.C;
     const real third = real(1.0 / 3.0);
 
@@ -575,17 +618,20 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
         const size_t slot = (size_t)env * Kc + kk;
         const int* wp = wpref + slot * (g.W + 1);
         const uint32_t* b = bits + slot * g.W;
+        // pieces of the record only: kb .. ke - 2 (n at the record's first sample uses its first piece)
+        const int kb = ep.n > 0 ? wp[ep.w0[rec]] : 0;
         const int cl0 = wp[n0 >> 5];
         const int nlast = n0 + nl - 1;
         const int wl = nlast >> 5, jl = nlast & 31;
         const int cll = wp[wl] + __popc(b[wl] & ((1u << jl) - 1u));
-        tab[idx * 3 + 0] = max(cl0 - 1, 0);
-        tab[idx * 3 + 1] = max(cll - 1, 0);
+        tab[idx * 3 + 0] = max(cl0 - 1, kb);
+        tab[idx * 3 + 1] = max(cll - 1, kb);
         tab[idx * 3 + 2] = cl0;
+        if (ep.n > 0) tab[6 * Kc + 1 + idx] = kb;
     }
     if (threadIdx.x < 32) {
         int q = 0;
-        for (int k = threadIdx.x; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        for (int k = threadIdx.x; k < g.K; k += 32) q += dir_qualifies(g, ep, cnt, k, rec) ? 1 : 0;
         q = warp_sum(q);
         if (threadIdx.x == 0) sQ[0] = q;
     }
@@ -603,7 +649,7 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
     for (int kk = 0; kk < Kc; ++kk) {
         const int k = k0 + kk;
         const int Emax = cnt[k], Emin = cnt[g.K + k];
-        if (!(Emax > 3 && Emin > 3)) continue;
+        if (!dir_qualifies(g, ep, cnt, k, rec)) continue;
         if (Emax > g.cap || Emin > g.cap) continue;
 #pragma unroll
         for (int env = 0; env < 2; ++env) {
@@ -634,7 +680,7 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
                 int cntl = 0;
                 for (int q = 0; q < w; ++q) cntl += __popc(wds[q]);
                 cntl += __popc(wds[w] & ((1u << jb) - 1u));
-                const int iv = max(cl0 + cntl - 1, 0);
+                const int iv = max(cl0 + cntl - 1, ep.n > 0 ? tab[6 * Kc + 1 + env * Kc + kk] : 0);
                 int li = iv - ia;
                 li = min(li, m - 1);
                 lis[t] = li;
@@ -692,7 +738,8 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
         }
     }
     const int Q = sQ[0];
-    if (!M && last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
+    if (!M && last_chunk && Q == 0 && (blockIdx.x == 0 || ep.n > 0) && blockIdx.y == 0 && threadIdx.x == 0)
+        atomicOr(&st->flags, 1);
     if (!cok) return;
 #pragma unroll
     for (int j = 0; j < SPT; ++j) {
@@ -1008,7 +1055,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
            const dd* __restrict__ rtab, const dd* __restrict__ rtab3, const dd* __restrict__ sv,
            const dd* __restrict__ yend, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear,
            const int* __restrict__ cumcfg, CumShared sh_g, Geom g, int k0, int Kc, int first_chunk, int last_chunk,
-           RunState* st)
+           RunState* st, Epochs ep)
 {
     constexpr int SUB = 32 / G;
     constexpr int NWS = 8 * SUB;
@@ -1031,8 +1078,13 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)
         for (int i = threadIdx.x; i < 2 * C; i += blockDim.x) bnd_clear[i] = 0u;
     if (w >= g.W) return;  // uniform over the CTA
+    // the record (epoch) of the span; spans never straddle two (epochs start at
+    // multiples of kEpochAlign = 512 samples, spans are at most 256 long)
+    const int rec = ep.n > 0 ? ep.wep[w] : 0;
+    const int rend = ep.n > 0 ? ep.off[rec] + ep.len[rec] : g.L;  // one past the record's last sample
     const int p0 = w * 32;
-    const int nl = min(32 * mw, g.L - p0);
+    if (p0 >= rend) return;  // gap between epochs
+    const int nl = min(32 * mw, rend - p0);
     const int ra = min(16 * mw, nl - 1);
     const int na = p0 + ra;
     const int c = blockIdx.y * G + cc;
@@ -1065,19 +1117,21 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
             if (ei < e_hi) {
                 const int kk = ei >> 1, env = ei & 1, k = k0 + kk;
                 const int Ex = cnt[k], En = cnt[g.K + k];
-                if (Ex > 3 && En > 3 && Ex <= g.cap && En <= g.cap) {
-                    const int E = env ? En : Ex;
+                if (Ex <= g.cap && En <= g.cap && dir_qualifies(g, ep, cnt, k, rec)) {
                     const size_t slot = (size_t)env * Kc + kk;
                     const uint32_t* bb = bits + slot * g.W;
                     const int* wp = wpref + slot * (g.W + 1);
+                    // the record's knots: kb .. ke - 1 (first and last at its end samples)
+                    const int kb = ep.n > 0 ? wp[ep.w0[rec]] : 0;
+                    const int ke = ep.n > 0 ? wp[ep.w0[rec + 1]] : (env ? En : Ex);
                     const uint32_t bw = bb[w];
                     const uint32_t bwa = bb[wa];
                     const uint32_t le = (ba == 31) ? bwa : (bwa & ((2u << ba) - 1u));
-                    i = min(wp[wa] + __popc(le) - 1, E - 2);
-                    j = max(1, wp[w] + (int)(bw & 1u));
+                    i = min(wp[wa] + __popc(le) - 1, ke - 2);
+                    j = max(kb + 1, wp[w] + (int)(bw & 1u));
                     int nw = wp[wend] - wp[w] - (int)(bw & 1u);  // knots in (p0, p0 + 32 m)
                     if (wend < g.W && nl == 32 * mw) nw += __popc(bb[wend] & 7u);
-                    n = max(0, min(j + nw - 1, E - 2) - j + 1);
+                    n = max(0, min(j + nw - 1, ke - 2) - j + 1);
                     const int* kn = knots + slot * g.cap;
                     xi = kn[i];
                     hh = kn[i + 1] - xi;
@@ -1105,10 +1159,11 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
             {
                 const int i = eI[le];
                 const int xi = eX[le], h = eH[le];
-                // knot values: X at interior knots, the clamped ends (samples 0 and L - 1) from yend
-                const dd* ye = yend + slot * 2 * (size_t)C + cl;
-                const dd y0 = (xi == 0) ? ye[0] : xval<dd>(X[(size_t)xi * C + cl]);
-                const dd y1 = (xi + h == g.L - 1) ? ye[C] : xval<dd>(X[(size_t)(xi + h) * C + cl]);
+                // knot values: X at interior knots, the record's clamped end knots from yend
+                const dd* ye = yend + (slot * (ep.n > 0 ? ep.n : 1) + rec) * 2 * (size_t)C + cl;
+                const int rbeg = ep.n > 0 ? ep.off[rec] : 0;
+                const dd y0 = (xi == rbeg) ? ye[0] : xval<dd>(X[(size_t)xi * C + cl]);
+                const dd y1 = (xi + h == rend - 1) ? ye[C] : xval<dd>(X[(size_t)(xi + h) * C + cl]);
                 const dd s0 = sv[rb + (size_t)i * C], s1 = sv[rb + (size_t)(i + 1) * C];
                 const dd d = (s1 - s0) * rtab3[h];
                 const dd s02(2.0f * s0.hi, 2.0f * s0.lo);  // exact
@@ -1210,7 +1265,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     }
     if (warp == 0) {
         int q = 0;
-        for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        for (int k = lane; k < g.K; k += 32) q += dir_qualifies(g, ep, cnt, k, rec) ? 1 : 0;
         q = warp_sum(q);
         if (lane == 0) sQ = q;
     }
@@ -1235,7 +1290,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     }
     __syncthreads();
     const int Q = sQ;
-    if (last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
+    if (last_chunk && Q == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
     for (int r = r0; r < r1; ++r) {  // in place: I(r) reads rows > r only
         const unsigned long long a1 = (r + 1 < r1) ? kq[(r + 1) * G + cc] : (r + 1 == r1 ? e0 : (r + 1 == r1 + 1 ? e1 : e2));
         const unsigned long long a2 = (r + 2 < r1) ? kq[(r + 2) * G + cc] : (r + 2 == r1 ? e0 : (r + 2 == r1 + 1 ? e1 : e2));
@@ -1333,7 +1388,7 @@ __device__ __forceinline__ bool df_gt(float2 a, float2 b) { return a.x > b.x || 
 
 __global__ void __launch_bounds__(256)
 k_project_mx(const float2* __restrict__ X, const float* __restrict__ dh_all, const float* __restrict__ dl_all,
-             uint32_t* __restrict__ bits, Geom g, int k0, int Kc, RunState* st)
+             uint32_t* __restrict__ bits, Geom g, int k0, int Kc, RunState* st, Epochs ep)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int C = g.C;
@@ -1401,10 +1456,8 @@ k_project_mx(const float2* __restrict__ X, const float* __restrict__ dh_all, con
     __syncthreads();
     const int n = n0 + sg * 32 + lane;
     const int r = 1 + sg * 32 + lane;
-    const int last = min(g.cov, g.L - 2);
-    const bool inrange = n < g.L;
-    const bool endpt = (n == 0) || (n == g.L - 1);
-    const bool interior = (n >= 1) && (n <= last);
+    bool inrange, endpt, interior;
+    sample_rule(g, ep, n, inrange, endpt, interior);
     const int w = (n0 >> 5) + sg;
     int refined = 0;
 #pragma unroll
@@ -1635,6 +1688,51 @@ __global__ void k_to_sample_major(const tin* __restrict__ y, XT* __restrict__ ru
     for (int r = threadIdx.y; r < 32; r += 8) {
         const int n = n_base + r, c = c_base + threadIdx.x;
         if (c < C && n < L) run[(size_t)n * C + c] = tile[threadIdx.x][r];
+    }
+}
+
+// Batched input: epoch e's record (C x len[e], channel-major, at y + yoff[e]
+// elements) -> the concatenated working signal run[off[e] + t][c].  One CTA
+// per (32-sample word, 32 channels); the gaps between epochs are left as they
+// are (zeroed by the caller).
+template <typename XT, typename tin>
+__global__ void k_batched_in(const tin* __restrict__ y, const long long* __restrict__ yoff, XT* __restrict__ run,
+                             int C, Epochs ep)
+{
+    __shared__ XT tile[32][33];
+    const int w = blockIdx.x;
+    const int e = ep.wep[w];
+    const int Le = ep.len[e];
+    const int t_base = w * 32 - ep.off[e], c_base = blockIdx.y * 32;
+    if (t_base >= Le) return;  // gap; uniform over the CTA
+    const tin* ye = y + yoff[e];
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int c = c_base + r, t = t_base + threadIdx.x;
+        if (c < C && t < Le) tile[r][threadIdx.x] = xfrom<XT>(ye[(size_t)c * Le + t]);
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int t = t_base + r, c = c_base + threadIdx.x;
+        if (c < C && t < Le) run[(size_t)(w * 32 + r) * C + c] = tile[threadIdx.x][r];
+    }
+}
+
+// Batched output: staged IMFs imf[i][c][n] (concatenated record) -> epoch e's
+// block out + nimf * yoff[e]: out[i][c][t] (nimf x C x len[e]).
+template <typename T>
+__global__ void k_batched_out(const T* __restrict__ imf, const long long* __restrict__ yoff, T* __restrict__ out,
+                              int C, int L, int nimf, Epochs ep)
+{
+    const long long total = (long long)nimf * C * L;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int n = (int)(idx % L);
+        const long long ic = idx / L;  // i * C + c
+        const int e = ep.wep[n >> 5];
+        const int t = n - ep.off[e], Le = ep.len[e];
+        if (t >= Le) continue;
+        const int c = (int)(ic % C), i = (int)(ic / C);
+        out[(long long)nimf * yoff[e] + ((long long)i * C + c) * Le + t] = imf[idx];
     }
 }
 

@@ -219,6 +219,20 @@ class Plan:
                   ctypes.byref(st) if stats else None))
         return st if stats else None
 
+    def run_batched(self, y, lengths, offsets, dirs, imfs, stream=None, stats: bool = True):
+        """Batched plan (max_epochs > 0): epoch e is y[offsets[e] : offsets[e] + C*lengths[e]]
+        (C x lengths[e], channel-major) of the 1-D device tensor y; its IMFs go to
+        imfs[num_imfs*offsets[e] : ...] (num_imfs x C x lengths[e])."""
+        n = len(lengths)
+        la = (ctypes.c_int64 * n)(*[int(v) for v in lengths])
+        oa = (ctypes.c_int64 * n)(*[int(v) for v in offsets])
+        st = Stats()
+        fn = lib().memd_run_batched_f64 if self.cfg.precision == PREC_F64 else lib().memd_run_batched_f32
+        _check(fn(self.handle, n, ctypes.cast(la, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p), _dptr(y),
+                  _dptr(dirs), _dptr(imfs), _stream_ptr(stream),
+                  ctypes.byref(st) if stats else None))
+        return st if stats else None
+
     def profile(self, y, dirs, imfs, stream=None) -> Profile:
         """Eager run with every kernel timed by CUDA events (per-stage ms)."""
         pr = Profile()

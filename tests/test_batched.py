@@ -1,0 +1,104 @@
+"""Batched runs: many epochs of uneven length decomposed in one pass
+(memd_run_batched_*), checked against one single-record run per epoch."""
+import numpy as np
+import pytest
+
+import memd_gb300 as mg
+import oracle
+
+
+def test_batched_plan_limits_on_host():
+    for kw in (dict(precision=mg.PREC_F32), dict(precision=mg.PREC_F64, stop_mode=mg.STOP_CRITERION),
+               dict(precision=mg.PREC_MIXED, mean_eval=1)):
+        with pytest.raises(mg.MemdError) as ei:
+            mg.Plan(4, 1000, 8, 3, 2, max_epochs=4, **kw)
+        assert ei.value.status == mg.MEMD_ERR_UNSUPPORTED
+    with pytest.raises(mg.MemdError) as ei:
+        mg.Plan(4, 1 << 20, 8, 3, 2, max_epochs=512)
+    assert ei.value.status == mg.MEMD_ERR_INVALID
+
+
+def _epochs(C, lengths, seed):
+    recs = [mg.synth_eeg(C, L, 256.0, seed=seed + e) for e, L in enumerate(lengths)]
+    offs = np.concatenate([[0], np.cumsum([C * L for L in lengths])[:-1]]).astype(np.int64)
+    return recs, offs
+
+
+def _run_batched(recs, lengths, offs, d, nimf, it, prec, **kw):
+    torch = pytest.importorskip("torch")
+    C = recs[0].shape[0]
+    tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
+    plan = mg.Plan(C, max(lengths), d.shape[0], nimf, it, precision=prec, max_epochs=len(lengths), **kw)
+    y = torch.as_tensor(np.concatenate([r.ravel() for r in recs]), dtype=tdt, device="cuda")
+    out = torch.full((nimf * y.numel(),), float("nan"), dtype=tdt, device="cuda")
+    dd = torch.as_tensor(d, dtype=tdt, device="cuda")
+    st = plan.run_batched(y, lengths, offs, dd, out)
+    o = out.cpu().numpy()
+    plan.close()
+    return [o[nimf * off: nimf * off + nimf * C * L].reshape(nimf, C, L) for off, L in zip(offs, lengths)], st
+
+
+def _run_single(rec, d, nimf, it, prec, **kw):
+    torch = pytest.importorskip("torch")
+    C, L = rec.shape
+    tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
+    plan = mg.Plan(C, L, d.shape[0], nimf, it, precision=prec, **kw)
+    out = torch.empty((nimf, C, L), dtype=tdt, device="cuda")
+    plan.run(torch.as_tensor(rec, dtype=tdt, device="cuda"), torch.as_tensor(d, dtype=tdt, device="cuda"), out)
+    o = out.cpu().numpy()
+    plan.close()
+    return o
+
+
+LENGTHS = [1000, 37, 512, 2049, 4096, 777, 1024]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("chunk", [0, 5])
+def test_batched_f64_equals_single_runs_bitwise(chunk):
+    """Epoch boundaries are identity rows of the spline systems and every
+    tile, span and bitmask word stays inside one epoch, so each epoch's IMFs
+    equal a single-record run of it bit for bit (FP64)."""
+    C, K, nimf, it = 6, 16, 4, 4
+    recs, offs = _epochs(C, LENGTHS, seed=50)
+    d = oracle.directions(C, K)
+    got, st = _run_batched(recs, LENGTHS, offs, d, nimf, it, mg.PREC_F64, dir_chunk=chunk)
+    for rec, g in zip(recs, got):
+        ref = _run_single(rec, d, nimf, it, mg.PREC_F64, dir_chunk=chunk)
+        assert np.array_equal(g, ref, equal_nan=True)
+
+
+@pytest.mark.gpu
+def test_batched_mixed_matches_single_runs_and_fp64():
+    C, K, nimf, it = 8, 24, 5, 5
+    lengths = [3000, 1500, 4100, 2048, 900]
+    recs, offs = _epochs(C, lengths, seed=70)
+    d = oracle.directions(C, K).astype(np.float32).astype(np.float64)
+    recs32 = [r.astype(np.float32) for r in recs]
+    got, st = _run_batched(recs32, lengths, offs, d, nimf, it, mg.PREC_MIXED)
+    ref64, _ = _run_batched([r.astype(np.float64) for r in recs32], lengths, offs, d, nimf, it, mg.PREC_F64)
+    assert st.flags == 0
+    for rec, g, r64 in zip(recs32, got, ref64):
+        single = _run_single(rec, d, nimf, it, mg.PREC_MIXED)
+        for i in range(nimf):
+            assert np.linalg.norm(g[i] - single[i]) <= 1e-6 * np.linalg.norm(single[i])
+            assert np.linalg.norm(g[i] - r64[i]) <= 1e-6 * np.linalg.norm(r64[i])
+
+
+@pytest.mark.gpu
+def test_batched_api_misuse():
+    torch = pytest.importorskip("torch")
+    plan = mg.Plan(4, 500, 8, 3, 2, max_epochs=2)
+    y = torch.zeros(4 * 500, dtype=torch.float64, device="cuda")
+    d = torch.as_tensor(oracle.directions(4, 8), device="cuda")
+    out = torch.zeros(3 * 4 * 500, dtype=torch.float64, device="cuda")
+    with pytest.raises(mg.MemdError) as ei:
+        plan.run(y.view(4, 500), d, out.view(3, 4, 500))
+    assert ei.value.status == mg.MEMD_ERR_UNSUPPORTED
+    with pytest.raises(mg.MemdError) as ei:
+        plan.run_batched(y, [600], [0], d, out)
+    assert ei.value.status == mg.MEMD_ERR_INVALID
+    with pytest.raises(mg.MemdError) as ei:
+        plan.run_batched(y, [100, 100, 100], [0, 400, 800], d, out)
+    assert ei.value.status == mg.MEMD_ERR_INVALID
+    plan.close()

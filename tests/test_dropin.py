@@ -18,7 +18,7 @@ STUB = os.path.join(REPO, "memd-gpu_gb300", "lib", "libmemd_mex_stub.so")
 
 
 def test_tools_built_and_cli_usage():
-    for name in ("sample_synthetic_signal", "memd_cli"):
+    for name in ("sample_synthetic_signal", "memd_cli", "memd_sweep"):
         assert os.access(os.path.join(BIN, name), os.X_OK), name
     r = subprocess.run([os.path.join(BIN, "memd_cli"), "--help"], capture_output=True, text=True)
     assert r.returncode == 0 and "--channels" in r.stderr
@@ -95,3 +95,25 @@ def test_mex_entry_matches_c_abi_with_mex_primes():
     # argument errors come back as MATLAB errors before any device access
     rc = S.mex_stub_call(C, K, 0, it, dy.data_ptr(), L, dx.data_ptr(), dp.data_ptr(), out.data_ptr())
     assert rc == 1 and b"memd:args" in S.mex_stub_last_error()
+
+
+def test_sweep_usage():
+    r = subprocess.run([os.path.join(BIN, "memd_sweep"), "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "--lengths" in r.stderr
+    r = subprocess.run([os.path.join(BIN, "memd_sweep"), "--precision", "f16"], capture_output=True, text=True)
+    assert r.returncode == 2
+
+
+@pytest.mark.gpu
+def test_sweep_prints_the_reference_table():
+    """The runBenchmark equivalent prints one "Channel, Length, DirVec, Time"
+    row per (channels, directions, length) point."""
+    r = subprocess.run([os.path.join(BIN, "memd_sweep"), "--channels", "4,8", "--directions", "8",
+                        "--lengths", "500:1500:500", "--imfs", "3", "--iter", "2", "--precision", "mixed"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert lines[0] == "Channel, Length, DirVec, Time"
+    rows = [tuple(x.strip() for x in l.split(",")) for l in lines[1:]]
+    assert [(int(a), int(b), int(c)) for a, b, c, _ in rows] == [(C, L, 8) for C in (4, 8) for L in (500, 1000, 1500)]
+    assert all(float(t) > 0 for *_, t in rows)

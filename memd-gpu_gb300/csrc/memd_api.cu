@@ -305,10 +305,24 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         const unsigned nb = (unsigned)((ns + kSolveThreads - 1) / kSolveThreads);
         unsigned* bcur = p->cum ? p->bnd + (size_t)(p->bpass & 1) * 2 * g.C : nullptr;
         lc.begin();
-        k_solve_fwd<R, XT><<<nb, kSolveThreads, 0, s>>>((const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g,
-                                                       k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
-                                                       p->cum ? (const XT*)p->X : nullptr, p->knots,
-                                                       p->cum ? (const R*)p->yend : nullptr, p->ep);
+        bool xm = false;
+        if constexpr (P == MEMD_PREC_MIXED) {
+            if (p->cum) {  // knot values from the working signal (the impulse-accumulation path)
+                xm = true;
+                if (p->ep.n == 0)
+                    k_solve_fwd<R, XT, true, false><<<nb, kSolveThreads, 0, s>>>(
+                        (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H,
+                        p->ngroups, bcur, (const XT*)p->X, p->knots, (const R*)p->yend, p->ep);
+                else
+                    k_solve_fwd<R, XT, true, true><<<nb, kSolveThreads, 0, s>>>(
+                        (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H,
+                        p->ngroups, bcur, (const XT*)p->X, p->knots, (const R*)p->yend, p->ep);
+            }
+        }
+        if (!xm)
+            k_solve_fwd<R, XT, false, false><<<nb, kSolveThreads, 0, s>>>(
+                (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H, p->ngroups,
+                bcur, nullptr, p->knots, nullptr, p->ep);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         k_solve_bwd<R><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0,
@@ -877,7 +891,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     p->cumG = C >= 32 ? 32 : (C > 8 ? 16 : 8);
     const size_t rb = (size_t)p->real_bytes;
     if (c.precision == MEMD_PREC_MIXED)
-        p->proj_smem = 4 * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2) + C + kProjTK);
+        p->proj_smem = 4 * ((size_t)(kProjTN + 2) * (C + 1) + 2 * (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2) + C + kProjTK);
     else
         p->proj_smem = rb * ((size_t)(kProjTN + 2) * (C + 1) + (size_t)kProjTK * C + (size_t)kProjTK * (kProjTN + 2));
     const size_t CL = (size_t)C * L;

@@ -274,6 +274,18 @@ __device__ __forceinline__ dd sqrt_(dd a) { return dd_sqrt(a); }
 __device__ __forceinline__ double fmat_(double a, float t, double c) { return __fma_rn(a, (double)t, c); }
 __device__ __forceinline__ float fmat_(float a, float t, float c) { return __fmaf_rn(a, t, c); }
 __device__ __forceinline__ dd fmat_(dd a, float t, dd c) { return dd_mulf(a, t) + c; }
+// 1/a: IEEE division for double and float (the FP64 and FP32 forms keep the
+// reference's arithmetic); for a double-float, the correctly rounded float
+// reciprocal refined by one Newton step with an fma residual (~47 bits, a
+// quarter of the instructions of the double-float division)
+__device__ __forceinline__ double recip_(double a) { return __ddiv_rn(1.0, a); }
+__device__ __forceinline__ float recip_(float a) { return __fdiv_rn(1.0f, a); }
+__device__ __forceinline__ dd recip_(dd a)
+{
+    const float x0 = __frcp_rn(a.hi);
+    const float e = __fmaf_rn(-a.lo, x0, __fmaf_rn(-a.hi, x0, 1.0f));  // 1 - a x0
+    return dd_renorm(x0, __fmul_rn(x0, e));
+}
 __device__ __forceinline__ bool is_zero(double v) { return v == 0.0; }
 __device__ __forceinline__ bool is_zero(float v) { return v == 0.0f; }
 __device__ __forceinline__ bool is_zero(dd v) { return v.hi == 0.0f; }

@@ -312,28 +312,41 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
     real cp = real(0);
     int xl = js > 0 ? x[js - 1] : 0;
     int xi = x[js];
-    for (int i = js; i < i1; ++i) {
-        const int xr = (i < E - 1) ? x[i + 1] : xi;
-        real l, d, u;
-        if (record_end_knot(ep, xi, i, E)) {  // natural end conditions: s = 0
-            l = real(0); d = real(1); u = real(0);
-        } else {
-            const int hl = xi - xl, hr = xr - xi;
-            l = real(hl); u = real(hr); d = real(2 * (hl + hr));
+    constexpr int FB = 8;  // knot positions loaded per batch (independent loads)
+    for (int base = js; base < i1; base += FB) {
+        int xs[FB];
+#pragma unroll
+        for (int k = 0; k < FB; ++k) {
+            const int i = base + k;
+            xs[k] = (i < i1 && i < E - 1) ? x[i + 1] : 0;
         }
-        const real gp = fmad_(-l, cp, d);
-        const real m = div_(real(1), gp);
-        cp = mul_(u, m);
-        if (i >= i0) {
-            Fac<real> o;
-            o.m = m;
-            o.lm = mul_(l, m);
-            o.cp = cp;
-            o.ih = (i < E - 1) ? rtab[xr - xi] : real(0);
-            f[i] = o;
+#pragma unroll
+        for (int k = 0; k < FB; ++k) {
+            const int i = base + k;
+            if (i < i1) {
+                const int xr = (i < E - 1) ? xs[k] : xi;
+                real l, d, u;
+                if (record_end_knot(ep, xi, i, E)) {  // natural end conditions: s = 0
+                    l = real(0); d = real(1); u = real(0);
+                } else {
+                    const int hl = xi - xl, hr = xr - xi;
+                    l = real(hl); u = real(hr); d = real(2 * (hl + hr));
+                }
+                const real gp = fmad_(-l, cp, d);
+                const real m = recip_(gp);
+                cp = mul_(u, m);
+                if (i >= i0) {
+                    Fac<real> o;
+                    o.m = m;
+                    o.lm = mul_(l, m);
+                    o.cp = cp;
+                    o.ih = (i < E - 1) ? rtab[xr - xi] : real(0);
+                    f[i] = o;
+                }
+                xl = xi;
+                xi = xr;
+            }
         }
-        xl = xi;
-        xi = xr;
     }
 }
 
@@ -392,17 +405,18 @@ __device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, i
     return it;
 }
 
-template <typename real, typename XT>
+template <typename real, typename XT, bool XM, bool EPB>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
             real* __restrict__ dbuf, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
             unsigned* __restrict__ bnd, const XT* __restrict__ X, const int* __restrict__ knots,
             const real* __restrict__ yend, Epochs ep)
 {
-    // X != nullptr: knot values read from the working signal, y_i = X[x_i]
-    // (interior knots) and yend (the clamped end knots of each record),
-    // instead of yv.  Rows of a record's end knots are the identity rows of
-    // the factorisation (lm == 0): their right-hand side is 0.
+    // XM: knot values read from the working signal, y_i = X[x_i] (interior
+    // knots) and yend (the clamped end knots of each record), instead of yv;
+    // EPB (with XM): batched epochs, a record's end knots found by position.
+    // Rows of a record's end knots are the identity rows of the
+    // factorisation (lm == 0): their right-hand side is 0.
     constexpr int B = kSolveBatch;
     const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
     if (!it.ok) return;  // uniform over the warp
@@ -412,31 +426,35 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     const int cl = min(it.c, C - 1);
     const size_t slot = (size_t)it.env * Kc + it.kk;
     const Fac<real>* f = fac + slot * g.cap;
-    const real* y = X ? nullptr : yv + slot * (size_t)g.cap * C + cl;
+    const real* y = XM ? nullptr : yv + slot * (size_t)g.cap * C + cl;
     const int* kn = knots + slot * g.cap;
-    const int nrec = ep.n > 0 ? ep.n : 1;
-    const real* ye = X ? yend + slot * nrec * 2 * (size_t)C + cl : nullptr;
-    // (X mode) knot r at sample n: its record and whether it is the record's
+    const int nrec = EPB ? ep.n : 1;
+    const real* ye = XM ? yend + slot * nrec * 2 * (size_t)C + cl : nullptr;
+    // (XM) knot r at sample n: its record and whether it is the record's
     // first (1) or last (2) knot
     auto endfl = [&](int r, int n, int& e) -> int {
-        if (ep.n == 0) {
+        if constexpr (!EPB) {
             e = 0;
             return r == 0 ? 1 : (r == E - 1 ? 2 : 0);
+        } else {
+            e = ep.wep[n >> 5];
+            const int o = ep.off[e];
+            return n == o ? 1 : (n == o + ep.len[e] - 1 ? 2 : 0);
         }
-        e = ep.wep[n >> 5];
-        const int o = ep.off[e];
-        return n == o ? 1 : (n == o + ep.len[e] - 1 ? 2 : 0);
     };
     auto yx = [&](int n, int fl, int e) -> real {
         if (fl) return ye[(size_t)e * 2 * C + (fl == 2 ? C : 0)];
         return xval<real>(X[(size_t)n * C + cl]);
     };
     auto yrow = [&](int r) -> real {
-        if (!X) return y[(size_t)r * C];
-        const int n = kn[r];
-        int e;
-        const int fl = endfl(r, n, e);
-        return yx(n, fl, e);
+        if constexpr (!XM) {
+            return y[(size_t)r * C];
+        } else {
+            const int n = kn[r];
+            int e;
+            const int fl = endfl(r, n, e);
+            return yx(n, fl, e);
+        }
     };
     real* o = dbuf + slot * (size_t)g.cap * C + cl;
     const int is = (H < 0) ? 0 : max(0, i0 - H);
@@ -454,18 +472,23 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
             fm = fr.m;
             flm = fr.lm;
             fih = fr.ih;
-            if (X && base + 1 + lane < E) {
+            if (XM && base + 1 + lane < E) {
                 fx = kn[base + 1 + lane];
-                ffl = endfl(base + 1 + lane, fx, fe);
+                if (EPB) ffl = endfl(base + 1 + lane, fx, fe);
             }
         }
         real yb[B];
-        if (X) {
+        if constexpr (XM) {
 #pragma unroll
             for (int k = 0; k < B; ++k) {
                 const int n = __shfl_sync(0xffffffffu, fx, k);
-                const int fl = __shfl_sync(0xffffffffu, ffl, k);
-                const int e = __shfl_sync(0xffffffffu, fe, k);
+                int fl, e;
+                if constexpr (EPB) {
+                    fl = __shfl_sync(0xffffffffu, ffl, k);
+                    e = __shfl_sync(0xffffffffu, fe, k);
+                } else {
+                    fl = endfl(base + 1 + k, n, e);
+                }
                 yb[k] = (k < nb && base + 1 + k < E) ? yx(n, fl, e) : real(0);
             }
         } else {
@@ -1398,6 +1421,7 @@ k_project_mx(const float2* __restrict__ X, const float* __restrict__ dh_all, con
     float* ps = ds + kProjTK * C;                          // TK x (TN + 2)
     float* mx = ps + kProjTK * (kProjTN + 2);              // C: max |x| over the tile
     float* bnd = mx + C;                                   // TK
+    float* dls = bnd + kProjTK;                            // TK x C (low words)
     const int n0 = blockIdx.x * kProjTN;
     const int kt0 = blockIdx.y * kProjTK;
     for (int idx = threadIdx.x; idx < (kProjTN + 2) * C; idx += blockDim.x) {
@@ -1409,27 +1433,43 @@ k_project_mx(const float2* __restrict__ X, const float* __restrict__ dh_all, con
         const int kk = idx / C, c = idx - kk * C;
         const int k = kt0 + kk;
         ds[idx] = (k < Kc) ? dh_all[(size_t)(k0 + k) * C + c] : 0.f;
+        dls[idx] = (k < Kc) ? dl_all[(size_t)(k0 + k) * C + c] : 0.f;
     }
     __syncthreads();
-    for (int c = threadIdx.x; c < C; c += blockDim.x) {
-        float m = 0.f;
-        for (int r = 0; r < kProjTN + 2; ++r) m = fmaxf(m, fabsf(xs[r * ldx + c]));
-        mx[c] = m;
-    }
-    __syncthreads();
-    if (threadIdx.x < kProjTK) {
-        const int k = kt0 + threadIdx.x;
-        float bh = 0.f, bl = 0.f;
-        if (k < Kc) {
-            for (int c = 0; c < C; ++c) {
-                bh = __fmaf_ru(fabsf(ds[threadIdx.x * C + c]), mx[c], bh);
-                bl = __fmaf_ru(fabsf(dl_all[(size_t)(k0 + k) * C + c]), mx[c], bl);
-            }
-        }
-        // error bound of each projection, with margin for the bound's own rounding
-        bnd[threadIdx.x] = 1.01f * ((float)(C + 2) * 5.9604645e-8f * bh + 1.0000002f * bl);
-    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // max |x| per channel over the tile: warp w takes rows w, w + 8, ...
+    for (int c0 = 0; c0 < C; c0 += 32) {
+        const int c = c0 + lane;
+        float m = 0.f;
+        if (c < C)
+            for (int r = warp; r < kProjTN + 2; r += 8) m = fmaxf(m, fabsf(xs[r * ldx + c]));
+        ps[warp * 32 + lane] = m;  // ps is free until the projections
+        __syncthreads();
+        if (warp == 0 && c < C) {
+            float t = ps[lane];
+#pragma unroll
+            for (int w8 = 1; w8 < 8; ++w8) t = fmaxf(t, ps[w8 * 32 + lane]);
+            mx[c] = t;
+        }
+        __syncthreads();
+    }
+    // error bound of each projection (warp w: directions 2w, 2w + 1; lanes
+    // over channels), with margin for the bound's own rounding
+    for (int j = 0; j < 2; ++j) {
+        const int kk = warp * 2 + j;
+        float bh = 0.f, bl = 0.f;
+        if (kt0 + kk < Kc)
+            for (int c = lane; c < C; c += 32) {
+                bh = __fmaf_ru(fabsf(ds[kk * C + c]), mx[c], bh);
+                bl = __fmaf_ru(fabsf(dls[kk * C + c]), mx[c], bl);
+            }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            bh = __fadd_ru(bh, __shfl_xor_sync(kFull, bh, o));
+            bl = __fadd_ru(bl, __shfl_xor_sync(kFull, bl, o));
+        }
+        if (lane == 0) bnd[kk] = 1.01f * ((float)(C + 2) * 5.9604645e-8f * bh + 1.0000002f * bl);
+    }
     const int sg = warp & 1, dg = warp >> 1;
     {
         const int r = 1 + sg * 32 + lane;

@@ -268,9 +268,11 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
          Epochs ep)
 {
     // cumcfg != nullptr (impulse-accumulation mean): block 0 picks the mean
-    // kernel's anchor span, 32 m samples (m the largest power of two <= 8 with
-    // 32 m <= 9 h, h the chunk's mean knot spacing), and splits each span's
-    // (direction, envelope) pairs over P = m CTAs
+    // kernel's anchor span, 32 m samples (m = 2 where 64 <= 2 h, h the chunk's
+    // mean knot spacing, else 1: rounding carried across a span grows by at
+    // most ~(32m/h)^2 = 4 over a direct evaluation, and the fixed-point
+    // quantum's error by (32m)^3/6), and splits each span's (direction,
+    // envelope) pairs over P = m CTAs
     if (cumcfg && blockIdx.x == 0 && threadIdx.x < 32) {
         int q = 0;
         long long et = 0;
@@ -287,7 +289,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             int m = 1;
             if (et > 0) {
                 const double h = (double)g.L * (2.0 * q) / (double)et;
-                while (m < 8 && 32.0 * (2 * m) <= 9.0 * h) m *= 2;
+                while (m < 2 && 32.0 * (2 * m) <= 2.0 * h) m *= 2;
             }
             cumcfg[0] = m;
             cumcfg[1] = m;
@@ -526,8 +528,12 @@ template <typename real>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, const real* __restrict__ dbuf,
             real* __restrict__ sv, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
-            unsigned* __restrict__ bnd)
+            unsigned* __restrict__ spanc, const int* __restrict__ cumcfg, const int* __restrict__ knots)
 {
+    // spanc != nullptr (impulse-accumulation mean): raise spanc[sp * C + c]
+    // (float bits) to h^2 (|s_i| + |s_{i+1}|) / 4 of every piece that meets
+    // span sp (32 m samples, m = cumcfg[0]): the curvature part of the bound
+    // on |S(n)| over the span (the linear interpolant plus h^2/8 max|S''|).
     constexpr int B = kSolveBatch;
     const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
     if (!it.ok) return;
@@ -539,16 +545,25 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     const Fac<real>* f = fac + slot * g.cap;
     const real* d = dbuf + slot * (size_t)g.cap * C + cl;
     real* o = sv + slot * (size_t)g.cap * C + cl;
+    const int* kn = knots + slot * g.cap;
     const int ie = (H < 0) ? E : min(E, i1 + H);
+    const int lgs = spanc ? 5 + __ffs(min(max(cumcfg[0], 1), 8)) - 1 : 0;  // log2(32 m), m <= 8
+    int xnext = (spanc && ie < E) ? kn[ie] : 0;  // position of the row after the current one
     real snext = real(0);
-    float spart = 0.0f;
+    int cur_sp = -1;       // span whose curvature bound is being gathered
+    float cur_b = 0.0f;
+    auto flush = [&]() {
+        if (cur_sp >= 0 && cok) atomicMax(&spanc[(size_t)cur_sp * C + it.c], __float_as_uint(cur_b * 1.01f));
+    };
     for (int top = ie - 1; top >= i0; top -= B) {
         const int nb = min(B, top - i0 + 1);
         real fcp = real(0), fih = real(0);
+        int fx = 0;
         if (lane < nb) {
             const Fac<real> fr = f[top - lane];
             fcp = fr.cp;
             fih = fr.ih;
+            if (spanc) fx = kn[top - lane];
         }
         real db[B];
 #pragma unroll
@@ -556,21 +571,33 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
 #pragma unroll
         for (int k = 0; k < B; ++k) {
             const real cp = shfl_idx_(fcp, k), ihr = shfl_idx_(fih, k);
+            const int x0 = spanc ? __shfl_sync(0xffffffffu, fx, k) : 0;  // position of row top - k
             if (k < nb) {
                 const int i = top - k;
                 const real sol = fmad_(-cp, snext, db[k]);
                 if (i < i1) {
                     if (cok) o[(size_t)i * C] = sol;
-                    if (bnd && i < E - 1) {
+                    if (spanc && i < E - 1) {
                         const float ih = magf(ihr);
-                        spart = fmaxf(spart, __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih));
+                        const float cb = __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih);
+                        // the piece [x0, xnext] meets spans xnext >> lgs down to x0 >> lgs
+                        for (int sp = xnext >> lgs; sp >= (x0 >> lgs); --sp) {
+                            if (sp != cur_sp) {
+                                flush();
+                                cur_sp = sp;
+                                cur_b = cb;
+                            } else {
+                                cur_b = fmaxf(cur_b, cb);
+                            }
+                        }
                     }
                 }
                 snext = sol;
+                xnext = x0;
             }
         }
     }
-    if (bnd && cok) atomicMax(&bnd[C + it.c], __float_as_uint(spart * 1.01f));
+    if (spanc) flush();
 }
 
 // ---------------------------------------------------------------------------
@@ -1010,9 +1037,11 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
 // plus the cubic that matches the anchor state, so all warps share it.
 // ---------------------------------------------------------------------------
 // The double-float v times 2^sh as a 64-bit two's-complement integer (|v 2^sh|
-// < 2^62; bits below the 48-bit combined mantissa are dropped), by integer
-// instructions only: the float-to-int64 conversion instructions run on the
-// FP64 pipe, 1/64 of the FP32 rate on this GPU.
+// < 2^62), rounded to nearest (ties up) from the 48-bit combined mantissa, by
+// integer instructions only: the float-to-int64 conversion instructions run on
+// the FP64 pipe, 1/64 of the FP32 rate on this GPU.  Rounding to nearest keeps
+// the conversions unbiased: a truncation's one-sided error accumulates over
+// the sifts of a decomposition.
 __device__ __forceinline__ unsigned long long qfix(dd v, int sh)
 {
     const unsigned uh = __float_as_uint(v.hi), ul = __float_as_uint(v.lo);
@@ -1024,11 +1053,13 @@ __device__ __forceinline__ unsigned long long qfix(dd v, int sh)
     if (ul >> 31) ml = -ml;
     // lo in units of 2^(eh - 174): ml 2^(el - eh + 24); |lo| <= ulp(hi) gives el <= eh - 23
     const int dl = eh - el - 24;
-    const int mlo = (dl < 0) ? ml * 2 : (dl < 31 ? (ml >> dl) : (ml < 0 ? -1 : 0));
+    const int mlo = (dl < 0) ? ml * 2 : (dl == 0 ? ml : (dl < 31 ? ((ml + (1 << (dl - 1))) >> dl) : 0));
     const long long comb = (long long)mh * (1ll << 24) + (long long)mlo;  // |comb| < 2^48
     const int s = eh - 174 + sh;                                           // value 2^sh = comb 2^s
-    const long long r = (s >= 0) ? (long long)((unsigned long long)comb << min(s, 63))
-                                 : (comb >> min(-s, 63));
+    long long r;
+    if (s >= 0) r = (long long)((unsigned long long)comb << min(s, 63));
+    else if (s > -63) r = (comb + (1ll << (-s - 1))) >> (-s);
+    else r = 0;
     return (unsigned long long)r;
 }
 
@@ -1048,14 +1079,30 @@ __device__ __forceinline__ float fix2f(unsigned long long a, int sh, unsigned lo
     if (be <= 0) return 0.0f;
     return __uint_as_float(((unsigned)be << 23) | ((unsigned)top & 0x7fffffu));
 }
-// the two's-complement integer v times 2^-sh as a double-float (~47 bits)
+// the non-negative integer a (< 2^40) times 2^-sh as a float, rounded to nearest
+__device__ __forceinline__ float fix2f_rn(unsigned long long a, int sh)
+{
+    if (a == 0ull) return 0.0f;
+    int msb = 63 - __clzll((long long)a);
+    int sd = msb - 23;
+    unsigned long long top = (sd > 0) ? ((a + (1ull << (sd - 1))) >> sd) : (a << -sd);
+    if (top >> 24) {  // the rounding carried into a new leading bit
+        top >>= 1;
+        ++msb;
+    }
+    const int be = msb - sh + 127;
+    if (be <= 0) return 0.0f;
+    return __uint_as_float(((unsigned)be << 23) | ((unsigned)top & 0x7fffffu));
+}
+// the two's-complement integer v times 2^-sh as a double-float: the high word
+// truncated to 24 bits, the rest rounded to nearest (~48 bits, unbiased)
 __device__ __forceinline__ dd fix2dd(unsigned long long v, int sh)
 {
     const bool neg = (long long)v < 0;
     const unsigned long long a = neg ? 0ull - v : v;
-    unsigned long long r1, r2;
+    unsigned long long r1;
     const float hi = fix2f(a, sh, &r1);
-    const float lo = fix2f(r1, sh, &r2);
+    const float lo = fix2f_rn(r1, sh);
     return neg ? dd(-hi, -lo) : dd(hi, lo);
 }
 
@@ -1077,8 +1124,8 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
            const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
            const dd* __restrict__ rtab, const dd* __restrict__ rtab3, const dd* __restrict__ sv,
            const dd* __restrict__ yend, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear,
-           const int* __restrict__ cumcfg, CumShared sh_g, Geom g, int k0, int Kc, int first_chunk, int last_chunk,
-           RunState* st, Epochs ep)
+           const unsigned* __restrict__ spanc, unsigned* __restrict__ spanc_clear, const int* __restrict__ cumcfg,
+           CumShared sh_g, Geom g, int k0, int Kc, int first_chunk, int last_chunk, RunState* st, Epochs ep)
 {
     constexpr int SUB = 32 / G;
     constexpr int NWS = 8 * SUB;
@@ -1100,6 +1147,9 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const int w = si * mw;
     if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)
         for (int i = threadIdx.x; i < 2 * C; i += blockDim.x) bnd_clear[i] = 0u;
+    // the next pass's span bounds (its spans may differ): CTA b clears row b
+    if (blockIdx.x < (unsigned)g.W && blockIdx.y == 0)
+        for (int i = threadIdx.x; i < C; i += blockDim.x) spanc_clear[(size_t)blockIdx.x * C + i] = 0u;
     if (w >= g.W) return;  // uniform over the CTA
     // the record (epoch) of the span; spans never straddle two (epochs start at
     // multiples of kEpochAlign = 512 samples, spans are at most 256 long)
@@ -1115,8 +1165,9 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const int cl = min(c, C - 1);  // loads of lanes past the last channel stay in bounds
     for (int i = threadIdx.x; i < (nl + 3) * G; i += blockDim.x) kq[i] = 0ull;
     for (int i = threadIdx.x; i < 4 * G; i += blockDim.x) anc[i] = 0ull;
-    // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex
-    const float B = __uint_as_float(bnd[cl]) + __uint_as_float(bnd[C + cl]);
+    // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex, B = max |y|
+    // (channel) + the curvature bound of the pieces that meet this span
+    const float B = __uint_as_float(bnd[cl]) + __uint_as_float(spanc[(size_t)si * C + cl]);
     const bool bad = !(B < INFINITY);
     int ex = 0;
     frexpf(__fmul_rn(B, (float)(2 * Kc)) * 1.0009765625f, &ex);

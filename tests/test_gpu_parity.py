@@ -280,3 +280,20 @@ def test_mixed_impulse_mean_nan_when_no_direction_qualifies():
     b, sb, _ = run_gpu(y, d, 2, 1, precision=mg.PREC_MIXED)
     assert sb.flags & mg.FLAG_NO_QUALIFIED_DIRECTION
     assert np.isnan(b[0]).all()
+
+
+def test_long_record_mixed_runs_and_matches_fp64():
+    """64 channels x 262,144 samples (the long-record length, past the
+    reference's int32 indexing at 256 directions): the mixed form runs without
+    overflow flags and its first IMFs follow the FP64 path's."""
+    C, L, K = 64, 262144, 32
+    y = mg.synth_eeg(C, L, 512.0, seed=9).astype(np.float32)
+    d = oracle.directions(C, K).astype(np.float32)
+    a, sa, ta = run_gpu(y.astype(np.float64), d.astype(np.float64), 3, 2, trace=True)
+    b, sb, tb = run_gpu(y, d, 3, 2, precision=mg.PREC_MIXED, trace=True)
+    assert sa.flags == 0 and sb.flags == 0
+    assert np.array_equal(ta["count"][:2, :2], tb["count"][:2, :2])
+    assert np.array_equal(ta["hash"][:2, :2], tb["hash"][:2, :2])
+    for i in range(3):
+        assert rel_l2(b[i], a[i]) < 1e-6, i
+    assert np.abs(b.astype(np.float64).sum(axis=0) - y).max() < 1e-4 * np.abs(y).max()

@@ -76,7 +76,6 @@ struct memd_plan {
     void* rtab;
     void* rtab3;  // impulse-accumulation mean: 1/(3h) as double-float
     unsigned* bnd;  // impulse-accumulation mean: [2 passes][2 parts][C] per-channel bounds (float bits)
-    unsigned* spanc;  // impulse-accumulation mean: [2 passes][W][C] per-span curvature bounds (float bits)
     int* cumcfg;    // impulse-accumulation mean: anchor span (words) and CTAs per span, set by the factor kernel
     // batched runs (cfg.max_epochs > 0): epochs concatenated at multiples of
     // kEpochAlign samples; ep describes the current call's layout (n = 0: one record)
@@ -186,8 +185,6 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
             if (p->cum) {
                 const unsigned* cur = p->bnd + (size_t)(p->bpass & 1) * 2 * g.C;
                 unsigned* other = p->bnd + (size_t)((p->bpass + 1) & 1) * 2 * g.C;
-                const unsigned* scur = p->spanc + (size_t)(p->bpass & 1) * g.W * g.C;
-                unsigned* sother = p->spanc + (size_t)((p->bpass + 1) & 1) * g.W * g.C;
 #define MEMD_CASE(G_)                                                                                              \
     if (p->cumG == G_) {                                                                                           \
         dim3 grid((unsigned)((g.W + kCumMaxWords - 1) / kCumMaxWords * kCumMaxWords),                             \
@@ -195,8 +192,7 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
         k_mean_cum<G_><<<grid, 256, sizeof(unsigned long long) * (32 * kCumMaxWords + 3) * G_, s>>>(               \
             (const float2*)p->X, (float2*)p->Xb, (dd*)p->acc, p->bits, p->wpref, p->knots, p->cnt,               \
                                             (const dd*)p->rtab, (const dd*)p->rtab3, (const dd*)p->sv,           \
-                                            (const dd*)p->yend, cur, other, scur, sother, p->cumcfg, p->cumsh, g, k0, \
-                                            kc, first,                                                             \
+                                            (const dd*)p->yend, cur, other, p->cumcfg, p->cumsh, g, k0, kc, first,\
                                             last, p->st, p->ep);                                                   \
         return;                                                                                                    \
     }
@@ -330,9 +326,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         k_solve_bwd<R><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0,
-                                                   kc, p->S, p->Ss, p->H, p->ngroups,
-                                                   p->cum ? p->spanc + (size_t)(p->bpass & 1) * p->g.W * g.C : nullptr,
-                                                   p->cumcfg, p->knots);
+                                                   kc, p->S, p->Ss, p->H, p->ngroups, bcur);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
@@ -374,10 +368,7 @@ static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
     p->bpass = 0;
     void* const x0 = p->X;
-    if (p->cum) {
-        cudaMemsetAsync(p->bnd, 0, sizeof(unsigned) * 4 * (size_t)g.C, s);
-        cudaMemsetAsync(p->spanc, 0, sizeof(unsigned) * 2 * (size_t)g.W * g.C, s);
-    }
+    if (p->cum) cudaMemsetAsync(p->bnd, 0, sizeof(unsigned) * 4 * (size_t)g.C, s);
     for (int i = 0; i + 1 < nimf; ++i) {
         cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, s);
         for (int j = 0; j < maxit; ++j) {
@@ -930,7 +921,6 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     if (p->cum) {
         ALLOC(p->rtab3, sizeof(dd) * (size_t)(Lh + 1));
         ALLOC(p->bnd, sizeof(unsigned) * 4 * (size_t)C);
-        ALLOC(p->spanc, sizeof(unsigned) * 2 * (size_t)p->g.W * C);
         ALLOC(p->cumcfg, sizeof(int) * 4);
         ALLOC(p->cumsh.kq, sizeof(unsigned long long) * 35 * (size_t)p->g.W * C);
         ALLOC(p->cumsh.anc, sizeof(unsigned long long) * 4 * (size_t)p->g.W * C);

@@ -268,10 +268,10 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
          Epochs ep)
 {
     // cumcfg != nullptr (impulse-accumulation mean): block 0 picks the mean
-    // kernel's anchor span, 32 m samples (m = 2 where 64 <= 2 h, h the chunk's
-    // mean knot spacing, else 1: rounding carried across a span grows by at
-    // most ~(32m/h)^2 = 4 over a direct evaluation, and the fixed-point
-    // quantum's error by (32m)^3/6), and splits each span's (direction,
+    // kernel's anchor span, 32 m samples (m the largest power of two <= 8 with
+    // 32 m <= 2 h, h the chunk's mean knot spacing, so that rounding carried
+    // across a span grows by at most ~(32m/h)^2 = 4 over a direct evaluation;
+    // at the densest knots m = 1), and splits each span's (direction,
     // envelope) pairs over P = m CTAs
     if (cumcfg && blockIdx.x == 0 && threadIdx.x < 32) {
         int q = 0;
@@ -289,7 +289,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             int m = 1;
             if (et > 0) {
                 const double h = (double)g.L * (2.0 * q) / (double)et;
-                while (m < 2 && 32.0 * (2 * m) <= 2.0 * h) m *= 2;
+                while (m < 8 && 32.0 * (2 * m) <= 2.0 * h) m *= 2;
             }
             cumcfg[0] = m;
             cumcfg[1] = m;
@@ -528,12 +528,8 @@ template <typename real>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, const real* __restrict__ dbuf,
             real* __restrict__ sv, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
-            unsigned* __restrict__ spanc, const int* __restrict__ cumcfg, const int* __restrict__ knots)
+            unsigned* __restrict__ bnd)
 {
-    // spanc != nullptr (impulse-accumulation mean): raise spanc[sp * C + c]
-    // (float bits) to h^2 (|s_i| + |s_{i+1}|) / 4 of every piece that meets
-    // span sp (32 m samples, m = cumcfg[0]): the curvature part of the bound
-    // on |S(n)| over the span (the linear interpolant plus h^2/8 max|S''|).
     constexpr int B = kSolveBatch;
     const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
     if (!it.ok) return;
@@ -545,25 +541,16 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     const Fac<real>* f = fac + slot * g.cap;
     const real* d = dbuf + slot * (size_t)g.cap * C + cl;
     real* o = sv + slot * (size_t)g.cap * C + cl;
-    const int* kn = knots + slot * g.cap;
     const int ie = (H < 0) ? E : min(E, i1 + H);
-    const int lgs = spanc ? 5 + __ffs(min(max(cumcfg[0], 1), 8)) - 1 : 0;  // log2(32 m), m <= 8
-    int xnext = (spanc && ie < E) ? kn[ie] : 0;  // position of the row after the current one
     real snext = real(0);
-    int cur_sp = -1;       // span whose curvature bound is being gathered
-    float cur_b = 0.0f;
-    auto flush = [&]() {
-        if (cur_sp >= 0 && cok) atomicMax(&spanc[(size_t)cur_sp * C + it.c], __float_as_uint(cur_b * 1.01f));
-    };
+    float spart = 0.0f;
     for (int top = ie - 1; top >= i0; top -= B) {
         const int nb = min(B, top - i0 + 1);
         real fcp = real(0), fih = real(0);
-        int fx = 0;
         if (lane < nb) {
             const Fac<real> fr = f[top - lane];
             fcp = fr.cp;
             fih = fr.ih;
-            if (spanc) fx = kn[top - lane];
         }
         real db[B];
 #pragma unroll
@@ -571,33 +558,21 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
 #pragma unroll
         for (int k = 0; k < B; ++k) {
             const real cp = shfl_idx_(fcp, k), ihr = shfl_idx_(fih, k);
-            const int x0 = spanc ? __shfl_sync(0xffffffffu, fx, k) : 0;  // position of row top - k
             if (k < nb) {
                 const int i = top - k;
                 const real sol = fmad_(-cp, snext, db[k]);
                 if (i < i1) {
                     if (cok) o[(size_t)i * C] = sol;
-                    if (spanc && i < E - 1) {
+                    if (bnd && i < E - 1) {
                         const float ih = magf(ihr);
-                        const float cb = __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih);
-                        // the piece [x0, xnext] meets spans xnext >> lgs down to x0 >> lgs
-                        for (int sp = xnext >> lgs; sp >= (x0 >> lgs); --sp) {
-                            if (sp != cur_sp) {
-                                flush();
-                                cur_sp = sp;
-                                cur_b = cb;
-                            } else {
-                                cur_b = fmaxf(cur_b, cb);
-                            }
-                        }
+                        spart = fmaxf(spart, __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih));
                     }
                 }
                 snext = sol;
-                xnext = x0;
             }
         }
     }
-    if (spanc) flush();
+    if (bnd && cok) atomicMax(&bnd[C + it.c], __float_as_uint(spart * 1.01f));
 }
 
 // ---------------------------------------------------------------------------
@@ -1124,8 +1099,8 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
            const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
            const dd* __restrict__ rtab, const dd* __restrict__ rtab3, const dd* __restrict__ sv,
            const dd* __restrict__ yend, const unsigned* __restrict__ bnd, unsigned* __restrict__ bnd_clear,
-           const unsigned* __restrict__ spanc, unsigned* __restrict__ spanc_clear, const int* __restrict__ cumcfg,
-           CumShared sh_g, Geom g, int k0, int Kc, int first_chunk, int last_chunk, RunState* st, Epochs ep)
+           const int* __restrict__ cumcfg, CumShared sh_g, Geom g, int k0, int Kc, int first_chunk, int last_chunk,
+           RunState* st, Epochs ep)
 {
     constexpr int SUB = 32 / G;
     constexpr int NWS = 8 * SUB;
@@ -1147,9 +1122,6 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const int w = si * mw;
     if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)
         for (int i = threadIdx.x; i < 2 * C; i += blockDim.x) bnd_clear[i] = 0u;
-    // the next pass's span bounds (its spans may differ): CTA b clears row b
-    if (blockIdx.x < (unsigned)g.W && blockIdx.y == 0)
-        for (int i = threadIdx.x; i < C; i += blockDim.x) spanc_clear[(size_t)blockIdx.x * C + i] = 0u;
     if (w >= g.W) return;  // uniform over the CTA
     // the record (epoch) of the span; spans never straddle two (epochs start at
     // multiples of kEpochAlign = 512 samples, spans are at most 256 long)
@@ -1165,9 +1137,8 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const int cl = min(c, C - 1);  // loads of lanes past the last channel stay in bounds
     for (int i = threadIdx.x; i < (nl + 3) * G; i += blockDim.x) kq[i] = 0ull;
     for (int i = threadIdx.x; i < 4 * G; i += blockDim.x) anc[i] = 0ull;
-    // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex, B = max |y|
-    // (channel) + the curvature bound of the pieces that meet this span
-    const float B = __uint_as_float(bnd[cl]) + __uint_as_float(spanc[(size_t)si * C + cl]);
+    // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex
+    const float B = __uint_as_float(bnd[cl]) + __uint_as_float(bnd[C + cl]);
     const bool bad = !(B < INFINITY);
     int ex = 0;
     frexpf(__fmul_rn(B, (float)(2 * Kc)) * 1.0009765625f, &ex);

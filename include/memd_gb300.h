@@ -71,6 +71,28 @@ typedef enum {
     MEMD_STOP_CRITERION = 1/* Rilling et al. 2003 thresholds (sd, sd2, tol) */
 } memd_stop_mode;
 
+typedef enum {
+    MEMD_SPLINE_NATURAL = 0,   /* zero second derivative at the end knots: the
+                                  reference's tridiagonal_setup
+                                  (memReducedEpochs_dev.cu:704-736) */
+    MEMD_SPLINE_NOT_A_KNOT = 1 /* continuous third derivative at the second and
+                                  second-to-last knots (MATLAB spline, as the
+                                  published MEMD uses it; the reference's unused
+                                  tridiagonal_setup_nak, :738-773); envelopes
+                                  with fewer than 4 knots stay natural */
+} memd_spline_end;
+
+typedef enum {
+    MEMD_BOUNDARY_REFERENCE = 0, /* both end samples are knots of both
+                                    envelopes, their values clamped by linear
+                                    extrapolation (memReducedEpochs_dev.cu:98-103,
+                                    447-486, 545-584) */
+    MEMD_BOUNDARY_MIRROR = 1     /* no forced end knots: two extrema per end
+                                    mirrored about the outermost extremum or the
+                                    end sample (Rilling, Flandrin & Goncalves
+                                    2003); no reference counterpart */
+} memd_boundary;
+
 typedef struct {
     int64_t channels;      /* C >= 1 */
     int64_t length;        /* L >= 4 (batched: maximum epoch length) */
@@ -89,12 +111,17 @@ typedef struct {
     int32_t solve_window;  /* tridiagonal halo in knots (0 = default; <0 = exact) */
     int32_t max_epochs;    /* batched runs: epochs per call (0 = single record) */
     int32_t mean_eval;     /* mean envelope: 0 = automatic (impulse accumulation
-                              for the mixed form in fixed mode, otherwise
-                              direct evaluation), 1 = direct evaluation of every
-                              envelope, 2 = impulse accumulation (mixed form,
-                              fixed mode only) */
+                              for the mixed form in fixed mode with the
+                              reference boundary, otherwise direct evaluation),
+                              1 = direct evaluation of every envelope,
+                              2 = impulse accumulation (mixed form, fixed mode,
+                              reference boundary only) */
+    int32_t spline_end;    /* memd_spline_end: end conditions of the envelope
+                              splines */
+    int32_t boundary;      /* memd_boundary: how the envelopes are closed at the
+                              record's ends */
     int32_t reserved32;
-    int64_t reserved[3];
+    int64_t reserved[2];
 } memd_config;
 
 typedef struct {

@@ -95,6 +95,7 @@ struct memd_plan {
     int* wpref;
     int* knots;
     int* cnt;
+    int* mir;       // mirror boundary: [K][kMirWords] mirrored end knots per direction
     RunState* st;
     int* coord_bad;
     int* host_flag;
@@ -173,9 +174,10 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
     if (p->evalG == G_ && p->evalSPT == S_) {                                                              \
         using Sh = EvalShape<R, G_, S_>;                                                                   \
         dim3 grid((unsigned)((g.L + Sh::T - 1) / Sh::T), (unsigned)((g.C + G_ - 1) / G_));                 \
-        k_eval<R, G_, S_><<<grid, 256, Sh::smem_bytes(p->Kc), s>>>(                                       \
+        k_eval<R, G_, S_><<<grid, 256, Sh::smem_bytes(p->Kc, g.mirror), s>>>(                             \
             (R*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const Fac<R>*)p->fac,            \
-            (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part, p->ep); \
+            (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part, p->ep, \
+            p->mir);                                                                                       \
         return;                                                                                            \
     }
         MEMD_EVAL_CASES(MEMD_CASE)
@@ -208,11 +210,12 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
         if (stopm)                                                                                         \
             k_eval_w<G_, S_, XT, R, true><<<grid, 256, Sh::smem_bytes(true), s>>>(                         \
                 (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
-                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part);  \
+                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part,   \
+                p->mir);                                                                                   \
         else                                                                                               \
             k_eval_w<G_, S_, XT, R, false><<<grid, 256, Sh::smem_bytes(false), s>>>(                       \
                 (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
-                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, nullptr, nullptr);        \
+                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, nullptr, nullptr, p->mir); \
         return;                                                                                            \
     }
         MEMD_EVALW_CASES(MEMD_CASE)
@@ -230,7 +233,7 @@ static cudaError_t set_attrs(memd_plan* p)
 #define MEMD_CASE(G_, S_)                                                                              \
     if (p->evalG == G_ && p->evalSPT == S_)                                                            \
         e = cudaFuncSetAttribute(k_eval<R, G_, S_>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
-                                 (int)EvalShape<R, G_, S_>::smem_bytes(p->Kc));
+                                 (int)EvalShape<R, G_, S_>::smem_bytes(p->Kc, p->g.mirror));
         MEMD_EVAL_CASES(MEMD_CASE)
 #undef MEMD_CASE
     } else {
@@ -288,10 +291,22 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
             k_project_extrema<R, XT><<<pg, 256, p->proj_smem, s>>>((const XT*)p->X, (const R*)p->dir, p->bits, g, k0, kc,
                                                                    p->ep);
         lc.end(MEMD_STAGE_PROJECT);
+        if (g.mirror) {
+            const unsigned mb = (unsigned)((32L * kc + 127) / 128);
+            lc.begin();
+            if constexpr (P == MEMD_PREC_MIXED)
+                k_mirror<float2, float, float2, true><<<mb, 128, 0, s>>>(
+                    p->bits, (const float2*)p->X, nullptr, (const float*)p->dir,
+                    (const float*)p->dir + (size_t)g.K * g.C, p->mir, g, k0, kc);
+            else
+                k_mirror<R, R, XT, false><<<mb, 128, 0, s>>>(p->bits, (const XT*)p->X, (const R*)p->dir, nullptr,
+                                                              nullptr, p->mir, g, k0, kc);
+            lc.end(MEMD_STAGE_PROJECT);
+        }
         lc.begin();
         k_compact<R, XT><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (R*)p->yv,
                                                             (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows,
-                                                            p->cum ? (R*)p->yend : nullptr, p->ep);
+                                                            p->cum ? (R*)p->yend : nullptr, p->ep, p->mir);
         lc.end(MEMD_STAGE_COMPACT);
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
@@ -326,7 +341,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         k_solve_bwd<R><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0,
-                                                   kc, p->S, p->Ss, p->H, p->ngroups, bcur);
+                                                   kc, p->S, p->Ss, p->H, p->ngroups, bcur, p->knots);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
@@ -347,7 +362,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
             (const R*)p->M, (const R*)p->amp, p->cnt, g, p->cfg.stop_sd, p->cfg.stop_sd2, p->st);
         lc.end(MEMD_STAGE_OTHER);
         lc.begin();
-        k_decide<<<1, 32, 0, s>>>(p->st, p->cnt, g, p->cfg.stop_tol, (int)p->cfg.max_iter, h_sift);
+        k_decide<<<1, 32, 0, s>>>(p->st, p->cnt, g, p->cfg.stop_tol, (int)p->cfg.max_iter, h_sift, p->mir);
         lc.end(MEMD_STAGE_OTHER);
         lc.begin();
         k_apply<R, XT><<<(unsigned)std::min<size_t>((CL + 255) / 256, 4096), 256, 0, s>>>((XT*)p->X, (const R*)p->M,
@@ -793,6 +808,12 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     if (c.stop_mode == MEMD_STOP_CRITERION && (c.max_iter < 1 || !(c.stop_sd > 0) || !(c.stop_sd2 > 0) || c.stop_tol < 0))
         return set_error(MEMD_ERR_INVALID, "plan: stop criterion needs max_iter >= 1 and positive thresholds");
     if (c.max_epochs < 0 || c.max_epochs > (1 << 20)) return set_error(MEMD_ERR_INVALID, "plan: bad max_epochs");
+    if (c.spline_end != MEMD_SPLINE_NATURAL && c.spline_end != MEMD_SPLINE_NOT_A_KNOT)
+        return set_error(MEMD_ERR_INVALID, "plan: bad spline_end");
+    if (c.boundary != MEMD_BOUNDARY_REFERENCE && c.boundary != MEMD_BOUNDARY_MIRROR)
+        return set_error(MEMD_ERR_INVALID, "plan: bad boundary");
+    if (c.max_epochs > 0 && (c.spline_end != MEMD_SPLINE_NATURAL || c.boundary != MEMD_BOUNDARY_REFERENCE))
+        return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for natural splines and the reference boundary");
     if (c.max_epochs > 0) {
         if (c.precision == MEMD_PREC_F32)
             return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the FP64 and mixed forms");
@@ -821,8 +842,10 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     p->g.L = L;
     p->g.K = K;
     p->g.W = (L + 31) / 32;
-    p->g.cap = p->batched ? L / 2 + 5 * (int)c.max_epochs + 4 : (L + 1) / 2 + 4;
+    p->g.cap = p->batched ? L / 2 + 5 * (int)c.max_epochs + 4 : (L + 1) / 2 + 4 + (c.boundary ? 4 : 0);
     p->g.cov = c.ref_window ? 240 * ((L + 241) / 242) : L;
+    p->g.nak = c.spline_end == MEMD_SPLINE_NOT_A_KNOT;
+    p->g.mirror = c.boundary == MEMD_BOUNDARY_MIRROR;
     p->Kc = (c.dir_chunk > 0) ? std::min<int>((int)c.dir_chunk, K) : K;
     if (p->batched && c.dir_chunk <= 0) {
         // keep each [2][Kc][cap][C] knot array under ~16 GB
@@ -882,10 +905,12 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         delete p;
         return set_error(MEMD_ERR_INVALID, "plan: mean_eval must be 0, 1 or 2");
     }
-    const bool cum_ok = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED;
+    const bool cum_ok = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED &&
+                        c.boundary == MEMD_BOUNDARY_REFERENCE;
     if (c.mean_eval == 2 && !cum_ok) {
         delete p;
-        return set_error(MEMD_ERR_UNSUPPORTED, "plan: impulse-accumulation mean needs the mixed form in fixed mode");
+        return set_error(MEMD_ERR_UNSUPPORTED,
+                         "plan: impulse-accumulation mean needs the mixed form in fixed mode with the reference boundary");
     }
     p->cum = cum_ok && c.mean_eval != 1;
     p->cumG = C >= 32 ? 32 : (C > 8 ? 16 : 8);
@@ -911,12 +936,14 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     ALLOC(p->wpref, sizeof(int) * 2 * Kc * (p->g.W + 1));
     ALLOC(p->knots, sizeof(int) * 2 * Kc * p->g.cap);
     ALLOC(p->cnt, sizeof(int) * 2 * (size_t)K);
+    if (p->g.mirror) ALLOC(p->mir, sizeof(int) * kMirWords * (size_t)K);
     ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
     if (!p->cum) ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
     else ALLOC(p->yend, rb * 2 * Kc * (size_t)std::max<int64_t>(1, c.max_epochs) * 2 * C);  // [2][Kc][epochs][2][C]
     ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
     ALLOC(p->dbuf, rb * 2 * Kc * p->g.cap * C);
-    const int Lh = p->batched ? std::max(p->Lrec, kEpochAlign) : L;  // longest knot gap
+    // longest knot gap: a record (epoch) length; mirrored knots reach 2L - 2
+    const int Lh = p->batched ? std::max(p->Lrec, kEpochAlign) : (p->g.mirror ? 2 * L : L);
     ALLOC(p->rtab, rb * (size_t)(Lh + 1));
     if (p->cum) {
         ALLOC(p->rtab3, sizeof(dd) * (size_t)(Lh + 1));

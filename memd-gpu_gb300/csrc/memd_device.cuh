@@ -1,6 +1,7 @@
 // memd_device.cuh -- device-side types and helpers shared by the MEMD kernels.
 #pragma once
 
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -149,6 +150,8 @@ struct Geom {
     int W;      // 32-bit words per direction bitmask = ceil(L / 32)
     int cap;    // knot capacity per (direction, envelope)
     int cov;    // last interior sample tested for extrema
+    int nak;    // not-a-knot end conditions (MEMD_SPLINE_NOT_A_KNOT)
+    int mirror; // mirrored end knots (MEMD_BOUNDARY_MIRROR)
 };
 
 // Batched runs: the epochs are concatenated along the sample axis, each
@@ -174,7 +177,7 @@ __device__ __forceinline__ void sample_rule(const Geom& g, const Epochs& ep, int
 {
     if (ep.n == 0) {
         inrange = n < g.L;
-        endpt = (n == 0) || (n == g.L - 1);
+        endpt = !g.mirror && ((n == 0) || (n == g.L - 1));
         interior = (n >= 1) && (n <= min(g.cov, g.L - 2));
         return;
     }
@@ -204,6 +207,13 @@ __device__ __forceinline__ bool dir_qualifies(const Geom& g, const Epochs& ep, c
     if (ep.n == 0) return cnt[k] > 3 && cnt[g.K + k] > 3;
     return ep.cnt[(size_t)k * ep.n + e] > 3 && ep.cnt[((size_t)g.K + k) * ep.n + e] > 3;
 }
+
+// Mirrored end knots of one direction (boundary mode MEMD_BOUNDARY_MIRROR),
+// written by k_mirror, [K][kMirWords] ints: the symmetry samples, the counts
+// of left / right mirrored knots per envelope (0 = maxima) and their source
+// samples in ascending order of mirrored position 2 sym - src.
+constexpr int kMirWords = 16;
+enum { kMirLsym = 0, kMirRsym = 1, kMirNl = 2, kMirNr = 4, kMirLsrc = 6, kMirRsrc = 10 };
 
 // Per-run device state (counters and sticky flags).
 struct RunState {
@@ -286,6 +296,11 @@ __device__ __forceinline__ dd recip_(dd a)
     const float e = __fmaf_rn(-a.lo, x0, __fmaf_rn(-a.hi, x0, 1.0f));  // 1 - a x0
     return dd_renorm(x0, __fmul_rn(x0, e));
 }
+// identity rows of the factorisation (natural end conditions, record ends)
+// carry m = 1 exactly; every other row has m <= 1/3 (pivot >= 3)
+__device__ __forceinline__ bool is_one(double v) { return v == 1.0; }
+__device__ __forceinline__ bool is_one(float v) { return v == 1.0f; }
+__device__ __forceinline__ bool is_one(dd v) { return v.hi == 1.0f && v.lo == 0.0f; }
 __device__ __forceinline__ bool is_zero(double v) { return v == 0.0; }
 __device__ __forceinline__ bool is_zero(float v) { return v == 0.0f; }
 __device__ __forceinline__ bool is_zero(dd v) { return v.hi == 0.0f; }

@@ -128,8 +128,12 @@ __global__ void __launch_bounds__(512)
 k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __restrict__ knots,
           int* __restrict__ cnt, real* __restrict__ yv, const XT* __restrict__ X,
           memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st, int trace_rows,
-          real* __restrict__ yend, Epochs ep)
+          real* __restrict__ yend, Epochs ep, const int* __restrict__ mir)
 {
+    // g.mirror: the knot list is [left mirrored | interior extrema | right
+    // mirrored] (mir from k_mirror); wpref and the bitmask count the interior
+    // extrema only, the knot values come from the mirrored knots' source
+    // samples, and the reference's end-point clamp does not apply.
     // yend != nullptr: the knot values are not gathered; only the two end
     // knots' values (clamped) are written, to yend[env][kk][2][C], and the
     // consumers read the interior knot values from X.
@@ -145,6 +149,8 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
     const uint32_t* b = bits + slot * g.W;
     int* wp = wpref + slot * (g.W + 1);
     int* kn = knots + slot * g.cap;
+    const int* mi = g.mirror ? mir + (size_t)(k0 + kk) * kMirWords : nullptr;
+    const int nlm = mi ? mi[kMirNl + env] : 0, nrm = mi ? mi[kMirNr + env] : 0;
     const int per = (g.W + blockDim.x - 1) / blockDim.x;
     const int wb = threadIdx.x * per, we = min(g.W, wb + per);
     int local = 0;
@@ -183,22 +189,36 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
             const int j = __ffs(word) - 1;
             word &= word - 1u;
             const int n = w * 32 + j;
-            if (run < g.cap) kn[run] = n;
+            if (nlm + run < g.cap) kn[nlm + run] = n;
             ++run;
             h += splitmix64((uint64_t)(uint32_t)n);
         }
     }
-    const int E = total_s;
+    const int Eint = total_s;
+    const int E = nlm + Eint + nrm;
     h = warp_sum<unsigned long long>(h);
     if (lane == 0) hsum[wid] = h;
     if (threadIdx.x == 0) {
-        wp[g.W] = E;
+        wp[g.W] = Eint;
         cnt[env * g.K + k0 + kk] = E;
         if (E > g.cap) atomicOr(&st->flags, 2);
     }
     __syncthreads();
+    unsigned long long hm = 0;  // hash of the mirrored knots
+    if (mi && threadIdx.x == 0) {
+        for (int j = 0; j < nlm; ++j) {
+            const int pos = 2 * mi[kMirLsym] - mi[kMirLsrc + 2 * env + j];
+            if (j < g.cap) kn[j] = pos;
+            hm += splitmix64((uint64_t)(uint32_t)pos);
+        }
+        for (int j = 0; j < nrm; ++j) {
+            const int pos = 2 * mi[kMirRsym] - mi[kMirRsrc + 2 * env + j];
+            if (nlm + Eint + j < g.cap) kn[nlm + Eint + j] = pos;
+            hm += splitmix64((uint64_t)(uint32_t)pos);
+        }
+    }
     if (trace && threadIdx.x == 0) {
-        unsigned long long t = 0;
+        unsigned long long t = hm;
         for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += hsum[i];
         memd_trace_entry e;
         e.count = E;
@@ -219,10 +239,16 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
         real* y = yv + slot * (size_t)g.cap * C;
         for (int idx = threadIdx.x; idx < E * C; idx += blockDim.x) {
             const int i = idx / C, c = idx - i * C;
-            y[idx] = xval<real>(X[(size_t)kn[i] * C + c]);
+            int src;
+            if (!mi) src = kn[i];
+            else if (i < nlm) src = mi[kMirLsrc + 2 * env + i];
+            else if (i >= nlm + Eint) src = mi[kMirRsrc + 2 * env + (i - nlm - Eint)];
+            else src = kn[i];
+            y[idx] = xval<real>(X[(size_t)src * C + c]);
         }
         __syncthreads();  // the raw end values are written before the clamped ones replace them
     }
+    if (mi) return;
     for (int idx = threadIdx.x; idx < nrec * C; idx += blockDim.x) {
         const int e = idx / C, c = idx - e * C;
         const int kb = ep.n > 0 ? wp[ep.w0[e]] : 0;
@@ -328,18 +354,28 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             if (i < i1) {
                 const int xr = (i < E - 1) ? xs[k] : xi;
                 real l, d, u;
+                int wn = 0, wd = 0;  // right-hand-side weight wn / wd of a not-a-knot row
                 if (record_end_knot(ep, xi, i, E)) {  // natural end conditions: s = 0
                     l = real(0); d = real(1); u = real(0);
                 } else {
                     const int hl = xi - xl, hr = xr - xi;
                     l = real(hl); u = real(hr); d = real(2 * (hl + hr));
+                    if (g.nak && E >= 4 && i == 1) {
+                        // s_0 eliminated by the not-a-knot condition d_0 = d_1
+                        l = real(0); d = real(hl + 2 * hr); u = real(hr - hl);
+                        wn = hr; wd = hl + hr;
+                    } else if (g.nak && E >= 4 && i == E - 2) {
+                        // s_{E-1} eliminated by d_{E-3} = d_{E-2}
+                        l = real(hl - hr); d = real(2 * hl + hr); u = real(0);
+                        wn = hl; wd = hl + hr;
+                    }
                 }
                 const real gp = fmad_(-l, cp, d);
                 const real m = recip_(gp);
                 cp = mul_(u, m);
                 if (i >= i0) {
                     Fac<real> o;
-                    o.m = m;
+                    o.m = wd ? mul_(m, div_(real(wn), real(wd))) : m;
                     o.lm = mul_(l, m);
                     o.cp = cp;
                     o.ih = (i < E - 1) ? rtab[xr - xi] : real(0);
@@ -505,7 +541,7 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 const real ynext = yb[k];
                 real slope = real(0), r = real(0);
                 if (i < E - 1) slope = mul_(sub_(ynext, yi), ih);
-                if (!is_zero(lm)) r = mul_(real(3), sub_(slope, slope_prev));
+                if (!is_one(m)) r = mul_(real(3), sub_(slope, slope_prev));
                 const real dcur = fmad_(-lm, dprev, mul_(m, r));
                 // rows before i0 only warm the recurrence up
                 if (i >= i0) {
@@ -528,8 +564,13 @@ template <typename real>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, const real* __restrict__ dbuf,
             real* __restrict__ sv, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
-            unsigned* __restrict__ bnd)
+            unsigned* __restrict__ bnd, const int* __restrict__ knots)
 {
+    // Not-a-knot end conditions (g.nak, E >= 4): rows 0 and E-1 were solved as
+    // identity rows; s_0 = s_1 + (h_0 / h_1)(s_1 - s_2) is applied at row 0,
+    // and s_{E-1} = s_{E-2} + (h_{E-2} / h_{E-3})(s_{E-2} - s_{E-3}) by the
+    // warp that owns row E-3 (its window always reaches row E-1, and row E-2
+    // does not depend on s_{E-1}), which also writes row E-1.
     constexpr int B = kSolveBatch;
     const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
     if (!it.ok) return;
@@ -541,8 +582,10 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     const Fac<real>* f = fac + slot * g.cap;
     const real* d = dbuf + slot * (size_t)g.cap * C + cl;
     real* o = sv + slot * (size_t)g.cap * C + cl;
+    const int* kn = knots + slot * g.cap;
+    const bool nak = g.nak && E >= 4;
     const int ie = (H < 0) ? E : min(E, i1 + H);
-    real snext = real(0);
+    real snext = real(0), snext2 = real(0);
     float spart = 0.0f;
     for (int top = ie - 1; top >= i0; top -= B) {
         const int nb = min(B, top - i0 + 1);
@@ -560,14 +603,23 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
             const real cp = shfl_idx_(fcp, k), ihr = shfl_idx_(fih, k);
             if (k < nb) {
                 const int i = top - k;
-                const real sol = fmad_(-cp, snext, db[k]);
+                real sol = fmad_(-cp, snext, db[k]);
+                if (nak && i == 0)
+                    sol = add_(snext, div_(mul_(sub_(snext, snext2), real(kn[1] - kn[0])), real(kn[2] - kn[1])));
                 if (i < i1) {
-                    if (cok) o[(size_t)i * C] = sol;
+                    if (cok && !(nak && i == E - 1)) o[(size_t)i * C] = sol;
                     if (bnd && i < E - 1) {
                         const float ih = magf(ihr);
                         spart = fmaxf(spart, __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih));
                     }
+                    if (nak && i == E - 3) {
+                        const int hb = kn[E - 1] - kn[E - 2];
+                        const real sl = add_(snext, div_(mul_(sub_(snext, sol), real(hb)), real(kn[E - 2] - kn[E - 3])));
+                        if (cok) o[(size_t)(E - 1) * C] = sl;
+                        if (bnd) spart = fmaxf(spart, 0.25f * (magf(snext) + magf(sl)) * (float)hb * (float)hb);
+                    }
                 }
+                snext2 = snext;
                 snext = sol;
             }
         }
@@ -593,11 +645,30 @@ struct EvalShape {
     static constexpr int NR = 256 / G;
     static constexpr int T = NR * SPT;
     static constexpr int MI = T / 2 + 4;
-    static size_t smem_bytes(int Kc)
+    static size_t smem_bytes(int Kc, bool mirror)
     {
-        return sizeof(real) * ((size_t)MI * 4 * G + T + MI) + sizeof(int) * ((size_t)(MI + 1) + T + T / 32 + 8 * Kc + 4);
+        return sizeof(real) * ((size_t)MI * 4 * G + T + MI) +
+               sizeof(int) * ((size_t)(MI + 1) + T + T / 32 + 8 * Kc + 4 + (mirror ? 10 * Kc : 0));
     }
 };
+
+// Mirror boundary: knots before sample n among the mirrored ones (positions
+// lp0 <= lp1 left, rp0 <= rp1 right; INT_MAX where absent).  The interval of
+// sample n is (this + interior knots before n) - 1, clamped to [0, E - 2].
+__device__ __forceinline__ int mirror_before(int n, int lp0, int lp1, int rp0, int rp1)
+{
+    return (lp0 < n) + (lp1 < n) + (rp0 < n) + (rp1 < n);
+}
+// the mirrored knot positions of a (direction, envelope) with E knots
+__device__ __forceinline__ void mirror_positions(const int* __restrict__ mi, const int* __restrict__ kn, int env, int E,
+                                                 int& lp0, int& lp1, int& rp0, int& rp1)
+{
+    const int nl = mi[kMirNl + env], nr = mi[kMirNr + env];
+    lp0 = nl > 0 ? kn[0] : INT_MAX;
+    lp1 = nl > 1 ? kn[1] : INT_MAX;
+    rp0 = nr > 0 ? kn[E - nr] : INT_MAX;
+    rp1 = nr > 1 ? kn[E - 1] : INT_MAX;
+}
 
 template <typename real, int G, int SPT>
 __global__ void __launch_bounds__(256)
@@ -605,9 +676,10 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
        const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
        const Fac<real>* __restrict__ fac, const real* __restrict__ sv, const real* __restrict__ yv, Geom g,
        int k0, int Kc, int first_chunk, int last_chunk, RunState* st, real* __restrict__ M,
-       real* __restrict__ part, Epochs ep)
+       real* __restrict__ part, Epochs ep, const int* __restrict__ mir)
 {
     // M == nullptr: fixed mode, the last chunk updates X in place.
+    // g.mirror: intervals count the mirrored knots too (mirror_before).
     // M != nullptr: stop mode, the last chunk writes the mean envelope to M and
     // every chunk writes part[cg][kk][n] = sum over this CTA's channels of
     // (U - L)^2 for the amplitude statistic.
@@ -623,6 +695,7 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
     uint32_t* wds = reinterpret_cast<uint32_t*>(lis + T);  // [T/32]
     int* tab = reinterpret_cast<int*>(wds + T / 32);  // [2*Kc][3]; batched: + [1] + [2*Kc] record knot bases
     int* sQ = tab + 6 * Kc;
+    int* mtab = tab + 8 * Kc + 4;                      // mirror: [2*Kc][5] lp0, lp1, rp0, rp1, E
 
     const int n0 = blockIdx.x * T;
     const int cg = blockIdx.y;
@@ -653,6 +726,21 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
         tab[idx * 3 + 1] = max(cll - 1, kb);
         tab[idx * 3 + 2] = cl0;
         if (ep.n > 0) tab[6 * Kc + 1 + idx] = kb;
+        if (g.mirror) {
+            const int E = cnt[env * g.K + k0 + kk];
+            int lp0 = INT_MAX, lp1 = INT_MAX, rp0 = INT_MAX, rp1 = INT_MAX;
+            if (E >= 2 && E <= g.cap) {
+                mirror_positions(mir + (size_t)(k0 + kk) * kMirWords, knots + slot * g.cap, env, E, lp0, lp1, rp0, rp1);
+                tab[idx * 3 + 0] = min(max(mirror_before(n0, lp0, lp1, rp0, rp1) + cl0 - 1, 0), E - 2);
+                tab[idx * 3 + 1] = min(max(mirror_before(nlast, lp0, lp1, rp0, rp1) + cll - 1, 0), E - 2);
+            }
+            int* mt = mtab + idx * 5;
+            mt[0] = lp0;
+            mt[1] = lp1;
+            mt[2] = rp0;
+            mt[3] = rp1;
+            mt[4] = E;
+        }
     }
     if (threadIdx.x < 32) {
         int q = 0;
@@ -705,7 +793,11 @@ k_eval(real* __restrict__ X, real* __restrict__ acc_buf, const uint32_t* __restr
                 int cntl = 0;
                 for (int q = 0; q < w; ++q) cntl += __popc(wds[q]);
                 cntl += __popc(wds[w] & ((1u << jb) - 1u));
-                const int iv = max(cl0 + cntl - 1, ep.n > 0 ? tab[6 * Kc + 1 + env * Kc + kk] : 0);
+                int iv = max(cl0 + cntl - 1, ep.n > 0 ? tab[6 * Kc + 1 + env * Kc + kk] : 0);
+                if (g.mirror) {
+                    const int* mt = mtab + (env * Kc + kk) * 5;
+                    iv = min(max(mirror_before(n0 + t, mt[0], mt[1], mt[2], mt[3]) + cl0 + cntl - 1, 0), mt[4] - 2);
+                }
                 int li = iv - ia;
                 li = min(li, m - 1);
                 lis[t] = li;
@@ -815,8 +907,9 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
          const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
          const R* __restrict__ rtab, const R* __restrict__ sv, const R* __restrict__ yv, Geom g,
          int k0, int Kc, int first_chunk, int last_chunk, RunState* st, R* __restrict__ M,
-         R* __restrict__ part)
+         R* __restrict__ part, const int* __restrict__ mir)
 {
+    // g.mirror: intervals count the mirrored knots too (mirror_before).
     using Sh = EvalWShape<G, SPL, R>;
     constexpr int T = Sh::T;
     constexpr int MI = Sh::MI;
@@ -868,8 +961,15 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
                 if (32 * q + 32 <= nlast) cnt_last += __popc(w);
                 else if (32 * q < nlast) cnt_last += __popc(w & ((1u << (nlast - 32 * q)) - 1u));
             }
-            const int ia = max(cl0 - 1, 0);
-            const int ib = max(cl0 + cnt_last - 1, 0);
+            int ia = max(cl0 - 1, 0);
+            int ib = max(cl0 + cnt_last - 1, 0);
+            const int Ee = cnt[env * g.K + k];
+            int lp0 = INT_MAX, lp1 = INT_MAX, rp0 = INT_MAX, rp1 = INT_MAX;
+            if (g.mirror) {
+                mirror_positions(mir + (size_t)k * kMirWords, knots + slot * g.cap, env, Ee, lp0, lp1, rp0, rp1);
+                ia = min(max(mirror_before(n0, lp0, lp1, rp0, rp1) + cl0 - 1, 0), Ee - 2);
+                ib = min(max(mirror_before(n0 + nlast, lp0, lp1, rp0, rp1) + cl0 + cnt_last - 1, 0), Ee - 2);
+            }
             int m = ib - ia + 1;
             if (m > MI - 1) {
                 overflow = true;
@@ -895,7 +995,9 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
             for (int j = 0; j < SPL; ++j) {
                 const int t = s_first + j;
                 if (t < nl && cok) {
-                    const int iv = max(cl0 + cntb - 1, 0);
+                    int iv = max(cl0 + cntb - 1, 0);
+                    if (g.mirror)
+                        iv = min(max(mirror_before(n0 + t, lp0, lp1, rp0, rp1) + cl0 + cntb - 1, 0), Ee - 2);
                     const int li = min(iv - ia, m - 1);
                     if (li != cur) {
                         R y0, s0;
@@ -1559,6 +1661,231 @@ k_project_mx(const float2* __restrict__ X, const float* __restrict__ dh_all, con
 // ---------------------------------------------------------------------------
 // amp[n] (+)= sum over qualified directions of the chunk of
 //             sqrt(sum over channel groups of part[g][kk][n]) / 2
+// ---------------------------------------------------------------------------
+// Mirrored end knots (boundary mode MEMD_BOUNDARY_MIRROR; no reference
+// counterpart: the mirror extension of Rilling, Flandrin & Goncalves 2003,
+// two extrema per end).  One warp per direction: the first and last three
+// interior maxima and minima from the bitmasks, the projection at the end
+// samples and at the outermost extrema (summed like the projection kernel:
+// fma over the channels in order; double-float for the mixed form), then the
+// rule below, written to mir[k].
+// Left end, leading maximum: if P(0) lies above the first minimum the knots
+// mirror about the first maximum (maxima 2..3, minima 1..2), otherwise about
+// sample 0, which joins the minima (maxima 1..2; minimum 1 and sample 0).  A
+// leading minimum is the same with the roles exchanged.  If the outermost
+// mirrored knot of either list stays inside the record, the symmetry point
+// moves to sample 0 and the list of the symmetry extremum's kind becomes its
+// first two extrema.  The right end is the mirror image.  Directions with
+// fewer than two interior maxima or minima (which never enter the mean) get
+// no mirrored knots.
+// ---------------------------------------------------------------------------
+// the first `want` (<= 3) set bits of b[0..W) in ascending order; warp-wide
+__device__ __forceinline__ int warp_first_bits(const uint32_t* __restrict__ b, int W, int want, int* out)
+{
+    const int lane = threadIdx.x & 31;
+    int found = 0;
+    for (int w0 = 0; w0 < W && found < want; w0 += 32) {
+        const int w = w0 + lane;
+        const uint32_t v = (w < W) ? b[w] : 0u;
+        const int c = __popc(v);
+        int inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += t;
+        }
+        const int tot = __shfl_sync(kFull, inc, 31);
+        const int exc = inc - c;
+        const int take = min(want - found, tot);
+        for (int r = 0; r < take; ++r) {
+            const unsigned m = __ballot_sync(kFull, exc <= r && r < inc);
+            const int sl = __ffs((int)m) - 1;
+            int pos = 0;
+            if (lane == sl) {
+                uint32_t x = v;
+                for (int j = exc; j < r; ++j) x &= x - 1u;
+                pos = w * 32 + __ffs((int)x) - 1;
+            }
+            out[found + r] = __shfl_sync(kFull, pos, sl);
+        }
+        found += take;
+    }
+    return found;
+}
+// the last `want` (<= 3) set bits of b[0..W) in descending order; warp-wide
+__device__ __forceinline__ int warp_last_bits(const uint32_t* __restrict__ b, int W, int want, int* out)
+{
+    const int lane = threadIdx.x & 31;
+    int found = 0;
+    for (int w0 = W - 1; w0 >= 0 && found < want; w0 -= 32) {
+        const int w = w0 - lane;
+        const uint32_t v = (w >= 0) ? b[w] : 0u;
+        const int c = __popc(v);
+        int inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += t;
+        }
+        const int tot = __shfl_sync(kFull, inc, 31);
+        const int exc = inc - c;
+        const int take = min(want - found, tot);
+        for (int r = 0; r < take; ++r) {
+            const unsigned m = __ballot_sync(kFull, exc <= r && r < inc);
+            const int sl = __ffs((int)m) - 1;
+            int pos = 0;
+            if (lane == sl) {
+                uint32_t x = v;
+                for (int j = exc; j < r; ++j) x ^= 1u << (31 - __clz((int)x));
+                pos = w * 32 + 31 - __clz((int)x);
+            }
+            out[found + r] = __shfl_sync(kFull, pos, sl);
+        }
+        found += take;
+    }
+    return found;
+}
+
+// projection of sample n on direction row d (summed like the projection kernels)
+template <typename real, typename XT>
+__device__ __forceinline__ real proj_at(const XT* __restrict__ X, const real* __restrict__ d, int n, int C)
+{
+    real acc = real(0);
+    for (int c = 0; c < C; ++c) acc = fmad_(xval<real>(X[(size_t)n * C + c]), d[c], acc);
+    return acc;
+}
+__device__ __forceinline__ bool mgt(double a, double b) { return a > b; }
+__device__ __forceinline__ bool mgt(float a, float b) { return a > b; }
+__device__ __forceinline__ bool mgt(float2 a, float2 b) { return df_gt(a, b); }
+
+// MX: mixed form (double-float signal, float direction words dh / dl)
+template <typename PT, typename real, typename XT, bool MX>
+__global__ void __launch_bounds__(128)
+k_mirror(const uint32_t* __restrict__ bits, const XT* __restrict__ X, const real* __restrict__ dir,
+         const float* __restrict__ dh_all, const float* __restrict__ dl_all, int* __restrict__ mir, Geom g, int k0,
+         int Kc)
+{
+    const int kk = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (kk >= Kc) return;  // uniform over the warp
+    const int lane = threadIdx.x & 31;
+    const int k = k0 + kk;
+    int fx[3], fn[3], lx[3], ln[3];  // first (ascending) / last (descending) maxima and minima
+    const int nfx = warp_first_bits(bits + (size_t)kk * g.W, g.W, 3, fx);
+    const int nfn = warp_first_bits(bits + (size_t)(Kc + kk) * g.W, g.W, 3, fn);
+    const int nlx = warp_last_bits(bits + (size_t)kk * g.W, g.W, 3, lx);
+    const int nln = warp_last_bits(bits + (size_t)(Kc + kk) * g.W, g.W, 3, ln);
+    int* out = mir + (size_t)k * kMirWords;
+    if (nfx < 2 || nfn < 2) {
+        if (lane < kMirWords) out[lane] = 0;
+        return;
+    }
+    const int last = g.L - 1;
+    // projections at 0, L-1, the first maximum / minimum, the last maximum / minimum
+    const int smp = lane == 0 ? 0 : (lane == 1 ? last : (lane == 2 ? fx[0] : (lane == 3 ? fn[0] : (lane == 4 ? lx[0] : ln[0]))));
+    PT pv{};
+    if (lane < 6) {
+        if constexpr (MX) pv = df_dot(X + (size_t)smp * g.C, dh_all + (size_t)k * g.C, dl_all + (size_t)k * g.C, g.C);
+        else pv = proj_at<real, XT>(X, dir + (size_t)k * g.C, smp, g.C);
+    }
+    PT pr[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        if constexpr (MX) pr[j] = make_float2(__shfl_sync(kFull, pv.x, j), __shfl_sync(kFull, pv.y, j));
+        else pr[j] = shfl_idx_(pv, j);
+    }
+    if (lane != 0) return;
+    const PT P0 = pr[0], PL = pr[1], Pfx = pr[2], Pfn = pr[3], Plx = pr[4], Pln = pr[5];
+    int nl[2], nr[2], ls[2][2], rs[2][2], lsym, rsym;
+    // rev(a[from:to]) of the first extrema f (ascending, nf known)
+    auto firstrev = [](const int* f, int nf, int from, int to, int* o) -> int {
+        int c = 0;
+        for (int i = min(to, nf) - 1; i >= from; --i) o[c++] = f[i];
+        return c;
+    };
+    if (fx[0] < fn[0]) {
+        if (mgt(P0, Pfn)) {
+            nl[0] = firstrev(fx, nfx, 1, 3, ls[0]);
+            nl[1] = firstrev(fn, nfn, 0, 2, ls[1]);
+            lsym = fx[0];
+        } else {
+            nl[0] = firstrev(fx, nfx, 0, 2, ls[0]);
+            nl[1] = firstrev(fn, nfn, 0, 1, ls[1]);
+            ls[1][nl[1]++] = 0;
+            lsym = 0;
+        }
+    } else {
+        if (mgt(Pfx, P0)) {
+            nl[0] = firstrev(fx, nfx, 0, 2, ls[0]);
+            nl[1] = firstrev(fn, nfn, 1, 3, ls[1]);
+            lsym = fn[0];
+        } else {
+            nl[0] = firstrev(fx, nfx, 0, 1, ls[0]);
+            ls[0][nl[0]++] = 0;
+            nl[1] = firstrev(fn, nfn, 0, 2, ls[1]);
+            lsym = 0;
+        }
+    }
+    if (2 * lsym - ls[0][0] > 0 || 2 * lsym - ls[1][0] > 0) {
+        if (lsym == fx[0]) nl[0] = firstrev(fx, nfx, 0, 2, ls[0]);
+        else nl[1] = firstrev(fn, nfn, 0, 2, ls[1]);
+        lsym = 0;
+    }
+    // the last extrema l (descending): rev(a[n-2:n]) = l[0], l[1]; rev(a[n-3:n-1]) = l[1], l[2]
+    auto last2 = [](const int* l, int nl_, int* o) -> int {
+        const int c = min(2, nl_);
+        for (int i = 0; i < c; ++i) o[i] = l[i];
+        return c;
+    };
+    auto prev2 = [](const int* l, int nl_, int* o) -> int {
+        const int c = min(2, nl_ - 1);
+        for (int i = 0; i < c; ++i) o[i] = l[1 + i];
+        return c;
+    };
+    if (lx[0] < ln[0]) {
+        if (mgt(Plx, PL)) {
+            nr[0] = last2(lx, nlx, rs[0]);
+            nr[1] = prev2(ln, nln, rs[1]);
+            rsym = ln[0];
+        } else {
+            rs[0][0] = last;
+            rs[0][1] = lx[0];
+            nr[0] = 2;
+            nr[1] = last2(ln, nln, rs[1]);
+            rsym = last;
+        }
+    } else {
+        if (mgt(PL, Pln)) {
+            nr[0] = prev2(lx, nlx, rs[0]);
+            nr[1] = last2(ln, nln, rs[1]);
+            rsym = lx[0];
+        } else {
+            nr[0] = last2(lx, nlx, rs[0]);
+            rs[1][0] = last;
+            rs[1][1] = ln[0];
+            nr[1] = 2;
+            rsym = last;
+        }
+    }
+    if (2 * rsym - rs[0][nr[0] - 1] < last || 2 * rsym - rs[1][nr[1] - 1] < last) {
+        if (rsym == lx[0]) nr[0] = last2(lx, nlx, rs[0]);
+        else nr[1] = last2(ln, nln, rs[1]);
+        rsym = last;
+    }
+    out[kMirLsym] = lsym;
+    out[kMirRsym] = rsym;
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        out[kMirNl + e] = nl[e];
+        out[kMirNr + e] = nr[e];
+        out[kMirLsrc + 2 * e] = ls[e][0];
+        out[kMirLsrc + 2 * e + 1] = nl[e] > 1 ? ls[e][1] : 0;
+        out[kMirRsrc + 2 * e] = rs[e][0];
+        out[kMirRsrc + 2 * e + 1] = nr[e] > 1 ? rs[e][1] : 0;
+    }
+    out[14] = 0;
+    out[15] = 0;
+}
+
 template <typename real>
 __global__ void k_amp(const real* __restrict__ part, real* __restrict__ amp, const int* __restrict__ cnt,
                       Geom g, int k0, int Kc, int groups, int first_chunk)
@@ -1628,7 +1955,7 @@ k_stop_stats(const real* __restrict__ M, const real* __restrict__ amp, const int
 // than 3 interior extrema ends the decomposition.  Drives the sift loop's
 // conditional WHILE node.
 __global__ void k_decide(RunState* st, const int* __restrict__ cnt, Geom g, double tol, int max_iter,
-                         cudaGraphConditionalHandle h_sift)
+                         cudaGraphConditionalHandle h_sift, const int* __restrict__ mir)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     int q = 0;
@@ -1636,7 +1963,15 @@ __global__ void k_decide(RunState* st, const int* __restrict__ cnt, Geom g, doub
     for (int k = 0; k < g.K; ++k) {
         const int a = cnt[k], b = cnt[g.K + k];
         if (a > 3 && b > 3) ++q;
-        if ((a - 2) + (b - 2) >= 3) few = false;
+        // interior extrema: the knots less the two end samples (reference
+        // boundary) or less the mirrored knots
+        int ia = a - 2, ib = b - 2;
+        if (g.mirror) {
+            const int* mi = mir + (size_t)k * kMirWords;
+            ia = a - mi[kMirNl] - mi[kMirNr];
+            ib = b - mi[kMirNl + 1] - mi[kMirNr + 1];
+        }
+        if (ia + ib >= 3) few = false;
     }
     st->q = q;
     unsigned cont = 0;

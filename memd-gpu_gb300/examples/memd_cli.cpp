@@ -4,12 +4,15 @@
 //
 //   memd_cli --in x.bin --channels C [--f64] [--directions K] [--imfs N]
 //            [--iter M] [--precision f64|f32|mixed] [--stop [--sd v --sd2 v --tol v]]
-//            [--mex-primes] [--full-window] --out mode_matrix.bin
+//            [--mex-primes] [--full-window] [--spline natural|nak]
+//            [--boundary reference|mirror] --out mode_matrix.bin
 //   memd_cli --synthetic eeg|tones --channels C --length L [--seed S] ...
 //
 // Input values are float32 unless --f64; the IMFs are written in the input's
 // type.  --mex-primes builds the direction set with the MEX convention (the
-// first C primes) instead of the standalone table.
+// first C primes) instead of the standalone table.  --spline nak selects
+// not-a-knot envelope splines, --boundary mirror the mirrored end extrema
+// (both off by default: the reference's natural splines and end clamp).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -26,12 +29,13 @@ static void usage()
     std::fprintf(stderr,
                  "usage: memd_cli (--in FILE | --synthetic eeg|tones --length L [--seed S]) --channels C\n"
                  "                [--f64] [--directions K] [--imfs N] [--iter M] [--precision f64|f32|mixed]\n"
-                 "                [--stop [--sd v] [--sd2 v] [--tol v]] [--mex-primes] [--full-window] --out FILE\n");
+                 "                [--stop [--sd v] [--sd2 v] [--tol v]] [--mex-primes] [--full-window]\n"
+                 "                [--spline natural|nak] [--boundary reference|mirror] --out FILE\n");
 }
 
 int main(int argc, char** argv)
 {
-    std::string in, out, synth, prec_s;
+    std::string in, out, synth, prec_s, spline_s, bound_s;
     int64_t C = 0, L = 0, K = 64, nimf = 9, iter = 10;
     uint64_t seed = 0;
     bool f64 = false, stop = false, mex = false, full = false;
@@ -62,6 +66,8 @@ int main(int argc, char** argv)
         else if (a == "--tol") tol = std::atof(next());
         else if (a == "--mex-primes") mex = true;
         else if (a == "--full-window") full = true;
+        else if (a == "--spline") spline_s = next();
+        else if (a == "--boundary") bound_s = next();
         else if (a == "--help" || a == "-h") {
             usage();
             return 0;
@@ -120,6 +126,16 @@ int main(int argc, char** argv)
         cfg.stop_tol = tol;
     }
     if (full) cfg.ref_window = 0;
+    if (!spline_s.empty() && spline_s != "natural" && spline_s != "nak") {
+        std::fprintf(stderr, "--spline natural|nak\n");
+        return 2;
+    }
+    if (!bound_s.empty() && bound_s != "reference" && bound_s != "mirror") {
+        std::fprintf(stderr, "--boundary reference|mirror\n");
+        return 2;
+    }
+    if (spline_s == "nak") cfg.spline_end = MEMD_SPLINE_NOT_A_KNOT;
+    if (bound_s == "mirror") cfg.boundary = MEMD_BOUNDARY_MIRROR;
     memd_plan* plan = nullptr;
     if (memd_plan_create(&cfg, &plan) != MEMD_OK) {
         std::fprintf(stderr, "plan: %s\n", memd_last_error());

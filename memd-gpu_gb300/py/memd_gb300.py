@@ -25,6 +25,8 @@ MEMD_ERR_UNSUPPORTED = 6
 
 PREC_F64, PREC_F32, PREC_MIXED = 0, 1, 2
 STOP_FIXED, STOP_CRITERION = 0, 1
+SPLINE_NATURAL, SPLINE_NOT_A_KNOT = 0, 1
+BOUNDARY_REFERENCE, BOUNDARY_MIRROR = 0, 1
 FLAG_NO_QUALIFIED_DIRECTION = 1
 FLAG_KNOT_OVERFLOW = 2
 
@@ -63,8 +65,10 @@ class Config(ctypes.Structure):
         ("solve_window", ctypes.c_int32),
         ("max_epochs", ctypes.c_int32),
         ("mean_eval", ctypes.c_int32),
+        ("spline_end", ctypes.c_int32),
+        ("boundary", ctypes.c_int32),
         ("reserved32", ctypes.c_int32),
-        ("reserved", ctypes.c_int64 * 3),
+        ("reserved", ctypes.c_int64 * 2),
     ]
 
 

@@ -16,7 +16,13 @@
  *                    at :1191-1195
  *   scan+compaction  memReducedEpochs_dev.cu:143-445 (a plain ordered walk)
  *   end-point clamp  memReducedEpochs_dev.cu:447-486, 545-584
- *   spline system    memReducedEpochs_dev.cu:704-736
+ *   spline system    memReducedEpochs_dev.cu:704-736 (natural); the not-a-knot
+ *                    option follows the intent of the unused
+ *                    tridiagonal_setup_nak (memReducedEpochs_dev.cu:738-773),
+ *                    with c_0 / c_{E-1} eliminated (no zero pivot at equal
+ *                    spacings) and MATLAB spline's end conditions
+ *   mirror option    no reference counterpart: mirrored extrema at both ends,
+ *                    two per end (Rilling, Flandrin & Goncalves 2003)
  *   tridiagonal      memReducedEpochs_dev.cu:1227-1241 (Thomas instead of the
  *                    closed cusparse gtsv2_nopivot)
  *   coefficients     memReducedEpochs_dev.cu:775-793
@@ -43,6 +49,8 @@ typedef struct {
     int32_t stop_mode;   /* 0: fixed max_iter sifts per IMF (reference); 1: stop criterion */
     double sd, sd2, tol; /* stop thresholds (theta1, theta2, alpha) */
     int32_t nthreads;
+    int32_t spline_end;  /* 0: natural (reference); 1: not-a-knot (MATLAB spline) */
+    int32_t boundary;    /* 0: forced end knots + clamp (reference); 1: mirrored extrema */
     int32_t reserved;
 } oracle_opts;
 
@@ -58,6 +66,8 @@ void oracle_default_opts(oracle_opts* o)
 #else
     o->nthreads = 1;
 #endif
+    o->spline_end = 0;
+    o->boundary = 0;
     o->reserved = 0;
 }
 
@@ -124,6 +134,26 @@ float oracle_radical_inverse(int32_t base, uint32_t i)
     return inv;
 }
 
+/* Mirrored end knots of one direction (boundary mode 1): for each envelope
+ * (0 = maxima, 1 = minima) up to two source samples per end, listed in
+ * ascending order of their mirrored position 2*sym - src. */
+typedef struct {
+    int32_t lsym, rsym;
+    int32_t nl[2], nr[2];
+    int32_t lsrc[2][2], rsrc[2][2];
+} oracle_mirror;
+
+/* out = a[to-1], a[to-2], ..., a[from] (from, to clamped to [0, n]); returns the count */
+static int32_t oracle_take_rev(const int32_t* a, int64_t n, int64_t from, int64_t to, int32_t* out)
+{
+    int32_t c = 0;
+    int64_t i;
+    if (from < 0) from = 0;
+    if (to > n) to = n;
+    for (i = to - 1; i >= from; --i) out[c++] = a[i];
+    return c;
+}
+
 /* ---- double instantiation ---- */
 #define REAL double
 #define SUFFIX f64
@@ -158,14 +188,37 @@ float oracle_radical_inverse(int32_t base, uint32_t i)
 #undef SIN
 #undef COS
 
-/* Single envelope, exposed for unit tests (spline reproduces cubics etc.). */
-int oracle_envelope_f64(const int32_t* pos, const double* val, int64_t E, int64_t L, double* out)
+/* Single envelope, exposed for unit tests (spline reproduces cubics etc.).
+ * nak: 0 natural, 1 not-a-knot end conditions. */
+int oracle_envelope_f64(const int32_t* pos, const double* val, int64_t E, int64_t L, double* out, int32_t nak)
 {
     double* ws;
     if (E < 2 || L < 1) return -1;
     ws = (double*)malloc(sizeof(double) * (size_t)(5 * E));
     if (!ws) return -2;
-    envelope_f64(pos, val, E, L, out, ws);
+    envelope_f64(pos, val, E, L, out, ws, nak);
     free(ws);
+    return 0;
+}
+
+/* Mirrored end knots of one direction, exposed for unit tests: the source
+ * samples of the left / right mirrored knots of each envelope (env 0 = maxima)
+ * and the two symmetry samples.  out[0..1] = lsym, rsym; out[2..5] = counts
+ * nl[0], nl[1], nr[0], nr[1]; out[6..13] = lsrc[env][j]; out[14..21] =
+ * rsrc[env][j] (ascending mirrored position). */
+int oracle_mirror_f64(const double* P, int64_t L, const int32_t* imax, int64_t nx, const int32_t* imin,
+                      int64_t nn, int32_t* out)
+{
+    oracle_mirror m;
+    int e, j;
+    if (nx < 2 || nn < 2 || L < 4) return -1;
+    mirror_f64(P, L, imax, nx, imin, nn, &m);
+    out[0] = m.lsym; out[1] = m.rsym;
+    out[2] = m.nl[0]; out[3] = m.nl[1]; out[4] = m.nr[0]; out[5] = m.nr[1];
+    for (e = 0; e < 2; ++e)
+        for (j = 0; j < 4; ++j) {
+            out[6 + e * 4 + j] = j < 2 ? m.lsrc[e][j] : 0;
+            out[14 + e * 4 + j] = j < 2 ? m.rsrc[e][j] : 0;
+        }
     return 0;
 }

@@ -17,8 +17,18 @@
 #define FN(name) CAT(name, SUFFIX)
 
 /* Cubic-spline envelope of one channel through the knots (pos[0..E-1],
- * val[0..E-1]) evaluated at n = 0..L-1.
+ * val[0..E-1], ascending; mirrored knots may lie outside 0..L-1) evaluated
+ * at n = 0..L-1.
  *   - natural end conditions                        REF:704-736 tridiagonal_setup
+ *     or, nak != 0 and E >= 4, not-a-knot (third derivative continuous at
+ *     x_1 and x_{E-2}; the intent of the unused tridiagonal_setup_nak,
+ *     REF:738-773): c_0 is eliminated with row 1, which becomes
+ *       (h0 + 2 h1) c_1 + (h1 - h0) c_2 = h1 r_1 / (h0 + h1),
+ *     and c_{E-1} with row E-2 (a = h_{E-3}, b = h_{E-2}):
+ *       (a - b) c_{E-3} + (2a + b) c_{E-2} = a r_{E-2} / (a + b);
+ *     rows 0 and E-1 stay identity rows and c_0, c_{E-1} follow from the
+ *     not-a-knot conditions after the solve (REF:738-773 keeps c_0 in row 0
+ *     instead, whose pivot h0^2 - h1^2 vanishes at equal spacings)
  *   - tridiagonal solve (Thomas, stands in for the
  *     closed cusparse<t>gtsv2_nopivot)              REF:1227-1241
  *   - coefficients                                  REF:775-793 spline_coefficients
@@ -27,7 +37,7 @@
  *     three FMAs nvcc forms                         REF:795-830 interpolate
  * ws must hold 5*E REALs. */
 static void FN(envelope_)(const int32_t* pos, const REAL* val, int64_t E, int64_t L,
-                          REAL* out, REAL* ws)
+                          REAL* out, REAL* ws, int nak)
 {
     REAL* lo = ws;
     REAL* mid = ws + E;
@@ -47,6 +57,17 @@ static void FN(envelope_)(const int32_t* pos, const REAL* val, int64_t E, int64_
             up[i] = (REAL)hr;
             lo[i] = (REAL)hl;
             rhs[i] = (REAL)3 * ((val[i + 1] - val[i]) / (REAL)hr - (val[i] - val[i - 1]) / (REAL)hl);
+            if (nak && E >= 4 && i == 1) {
+                mid[i] = (REAL)(hl + 2 * hr);
+                up[i] = (REAL)(hr - hl);
+                lo[i] = 0;
+                rhs[i] = rhs[i] * (REAL)hr / (REAL)(hl + hr);
+            } else if (nak && E >= 4 && i == E - 2) {
+                mid[i] = (REAL)(2 * hl + hr);
+                up[i] = 0;
+                lo[i] = (REAL)(hl - hr);
+                rhs[i] = rhs[i] * (REAL)hl / (REAL)(hl + hr);
+            }
         }
     }
     /* Thomas elimination without pivoting; the system is strictly diagonally
@@ -60,6 +81,14 @@ static void FN(envelope_)(const int32_t* pos, const REAL* val, int64_t E, int64_
     }
     for (i = E - 2; i >= 0; --i) rhs[i] = rhs[i] - cp[i] * rhs[i + 1];
     /* rhs now holds the solution s_i (the reference's d_solutionGtsv). */
+    if (nak && E >= 4) {
+        /* d_0 = d_1:       c_0 = c_1 + (h0 / h1) (c_1 - c_2)
+         * d_{E-3} = d_{E-2}: c_{E-1} = c_{E-2} + (b / a) (c_{E-2} - c_{E-3}) */
+        int32_t h0 = pos[1] - pos[0], h1 = pos[2] - pos[1];
+        int32_t a = pos[E - 2] - pos[E - 3], b = pos[E - 1] - pos[E - 2];
+        rhs[0] = rhs[1] + (rhs[1] - rhs[2]) * (REAL)h0 / (REAL)h1;
+        rhs[E - 1] = rhs[E - 2] + (rhs[E - 2] - rhs[E - 3]) * (REAL)b / (REAL)a;
+    }
     {
         int64_t iv = 0;
         REAL a = val[0], b = 0, c = 0, d = 0;
@@ -155,23 +184,100 @@ int FN(oracle_directions_)(int64_t C, int64_t K, const int32_t* primes, REAL* di
 
 /* Extrema of one projected direction (REF:77-141 find_extrema_shfl_max/min,
  * compaction REF:384-445): strict local maxima (minima) at interior samples
- * n <= cov, plus both end samples.  Returns the knot count. */
-static int64_t FN(extrema_)(const REAL* P, int64_t L, int64_t cov, int is_max, int32_t* pos)
+ * n <= cov, plus both end samples when ends != 0.  Returns the count. */
+static int64_t FN(extrema_)(const REAL* P, int64_t L, int64_t cov, int is_max, int32_t* pos, int ends)
 {
     int64_t E = 0, n, last = L - 2;
     if (cov < last) last = cov;
-    pos[E++] = 0;
+    if (ends) pos[E++] = 0;
     for (n = 1; n <= last; ++n) {
         REAL v = P[n], l = P[n - 1], r = P[n + 1];
         if (is_max ? (v > l && v > r) : (v < l && v < r)) pos[E++] = (int32_t)n;
     }
-    if (L - 1 > 0) pos[E++] = (int32_t)(L - 1);
+    if (ends && L - 1 > 0) pos[E++] = (int32_t)(L - 1);
     return E;
 }
 
+/* Mirrored end knots (boundary mode 1; no reference counterpart, the method
+ * of Rilling, Flandrin & Goncalves 2003 with two extrema per end).  Inputs:
+ * the interior maxima imx[0..nx-1] and minima imn[0..nn-1] (ascending,
+ * nx >= 2, nn >= 2) of the projection P.
+ * Left end: when the first extremum is a maximum and P[0] lies above the
+ * first minimum, the knots mirror about that maximum (the next two maxima and
+ * the first two minima); otherwise sample 0 acts as a minimum: the knots
+ * mirror about sample 0 (the first two maxima; the first minimum and sample 0
+ * itself).  The case of a leading minimum is the same with the roles
+ * exchanged.  If a list's outermost mirrored knot then falls inside the
+ * record (position > 0), the symmetry point moves to sample 0 and the list
+ * of the symmetry extremum's kind becomes its first two extrema.  The right
+ * end is the mirror image of this rule. */
+static void FN(mirror_)(const REAL* P, int64_t L, const int32_t* imx, int64_t nx, const int32_t* imn, int64_t nn,
+                        oracle_mirror* m)
+{
+    const int32_t last = (int32_t)(L - 1);
+    if (imx[0] < imn[0]) {
+        if (P[0] > P[imn[0]]) {
+            m->nl[0] = oracle_take_rev(imx, nx, 1, 3, m->lsrc[0]);
+            m->nl[1] = oracle_take_rev(imn, nn, 0, 2, m->lsrc[1]);
+            m->lsym = imx[0];
+        } else {
+            m->nl[0] = oracle_take_rev(imx, nx, 0, 2, m->lsrc[0]);
+            m->nl[1] = oracle_take_rev(imn, nn, 0, 1, m->lsrc[1]);
+            m->lsrc[1][m->nl[1]++] = 0;
+            m->lsym = 0;
+        }
+    } else {
+        if (P[0] < P[imx[0]]) {
+            m->nl[0] = oracle_take_rev(imx, nx, 0, 2, m->lsrc[0]);
+            m->nl[1] = oracle_take_rev(imn, nn, 1, 3, m->lsrc[1]);
+            m->lsym = imn[0];
+        } else {
+            m->nl[0] = oracle_take_rev(imx, nx, 0, 1, m->lsrc[0]);
+            m->lsrc[0][m->nl[0]++] = 0;
+            m->nl[1] = oracle_take_rev(imn, nn, 0, 2, m->lsrc[1]);
+            m->lsym = 0;
+        }
+    }
+    if (2 * m->lsym - m->lsrc[0][0] > 0 || 2 * m->lsym - m->lsrc[1][0] > 0) {
+        if (m->lsym == imx[0]) m->nl[0] = oracle_take_rev(imx, nx, 0, 2, m->lsrc[0]);
+        else m->nl[1] = oracle_take_rev(imn, nn, 0, 2, m->lsrc[1]);
+        m->lsym = 0;
+    }
+    if (imx[nx - 1] < imn[nn - 1]) {
+        if (P[last] < P[imx[nx - 1]]) {
+            m->nr[0] = oracle_take_rev(imx, nx, nx - 2, nx, m->rsrc[0]);
+            m->nr[1] = oracle_take_rev(imn, nn, nn - 3, nn - 1, m->rsrc[1]);
+            m->rsym = imn[nn - 1];
+        } else {
+            m->rsrc[0][0] = last;
+            m->nr[0] = 1 + oracle_take_rev(imx, nx, nx - 1, nx, m->rsrc[0] + 1);
+            m->nr[1] = oracle_take_rev(imn, nn, nn - 2, nn, m->rsrc[1]);
+            m->rsym = last;
+        }
+    } else {
+        if (P[last] > P[imn[nn - 1]]) {
+            m->nr[0] = oracle_take_rev(imx, nx, nx - 3, nx - 1, m->rsrc[0]);
+            m->nr[1] = oracle_take_rev(imn, nn, nn - 2, nn, m->rsrc[1]);
+            m->rsym = imx[nx - 1];
+        } else {
+            m->nr[0] = oracle_take_rev(imx, nx, nx - 2, nx, m->rsrc[0]);
+            m->rsrc[1][0] = last;
+            m->nr[1] = 1 + oracle_take_rev(imn, nn, nn - 1, nn, m->rsrc[1] + 1);
+            m->rsym = last;
+        }
+    }
+    if (2 * m->rsym - m->rsrc[0][m->nr[0] - 1] < last || 2 * m->rsym - m->rsrc[1][m->nr[1] - 1] < last) {
+        if (m->rsym == imx[nx - 1]) m->nr[0] = oracle_take_rev(imx, nx, nx - 2, nx, m->rsrc[0]);
+        else m->nr[1] = oracle_take_rev(imn, nn, nn - 2, nn, m->rsrc[1]);
+        m->rsym = last;
+    }
+}
+
 typedef struct {
-    int32_t* pos[2];   /* per direction: knots (max, min), K*L each */
-    int64_t* cnt;      /* K*2 */
+    int32_t* pos[2];   /* per direction: knot positions (max, min), K*(L+4) each */
+    int32_t* src[2];   /* per direction: the sample each knot takes its value from */
+    int64_t* cnt;      /* K*2 knots */
+    int64_t* nint;     /* K*2 interior extrema */
     REAL* P;           /* K*L projections */
     REAL* acc;         /* C*L running sum of mean envelopes */
     REAL* amp;         /* L (stop mode) */
@@ -194,6 +300,7 @@ static int64_t FN(mean_envelope_)(int64_t C, int64_t L, int64_t K, const REAL* c
     int64_t cov = o->ref_window ? oracle_window_cover(L) : L;
     int64_t k, q = 0;
     int64_t i;
+    const int64_t LS = L + 4;  /* knot stride per direction */
     for (i = 0; i < C * L; ++i) w->acc[i] = 0;
     if (want_amp) for (i = 0; i < L; ++i) w->amp[i] = 0;
 #pragma omp parallel for schedule(static) num_threads(w->nthreads)
@@ -205,8 +312,41 @@ static int64_t FN(mean_envelope_)(int64_t C, int64_t L, int64_t K, const REAL* c
             for (c = 0; c < C; ++c) s = FMA(cur[c * L + n], dir[k * C + c], s);
             P[n] = s;
         }
-        w->cnt[2 * k + 0] = FN(extrema_)(P, L, cov, 1, w->pos[0] + k * L);
-        w->cnt[2 * k + 1] = FN(extrema_)(P, L, cov, 0, w->pos[1] + k * L);
+        if (!o->boundary) {
+            w->cnt[2 * k + 0] = FN(extrema_)(P, L, cov, 1, w->pos[0] + k * LS, 1);
+            w->cnt[2 * k + 1] = FN(extrema_)(P, L, cov, 0, w->pos[1] + k * LS, 1);
+            w->nint[2 * k + 0] = w->cnt[2 * k + 0] - 2;
+            w->nint[2 * k + 1] = w->cnt[2 * k + 1] - 2;
+        } else {
+            /* interior extrema, then (qualifying directions) the mirrored
+             * knots: [left mirrored | interior | right mirrored] */
+            oracle_mirror m;
+            int32_t* sx = w->src[0] + k * LS;
+            int32_t* sn = w->src[1] + k * LS;
+            int64_t ni[2];
+            int e;
+            ni[0] = FN(extrema_)(P, L, cov, 1, sx + 2, 0);
+            ni[1] = FN(extrema_)(P, L, cov, 0, sn + 2, 0);
+            memset(&m, 0, sizeof(m));
+            if (ni[0] >= 2 && ni[1] >= 2) FN(mirror_)(P, L, sx + 2, ni[0], sn + 2, ni[1], &m);
+            for (e = 0; e < 2; ++e) {
+                int32_t* sr = e ? sn : sx;
+                int32_t* ps = w->pos[e] + k * LS;
+                int64_t j, E;
+                memmove(sr + m.nl[e], sr + 2, sizeof(int32_t) * (size_t)ni[e]);
+                for (j = 0; j < m.nl[e]; ++j) sr[j] = m.lsrc[e][j];
+                for (j = 0; j < m.nr[e]; ++j) sr[m.nl[e] + ni[e] + j] = m.rsrc[e][j];
+                E = m.nl[e] + ni[e] + m.nr[e];
+                for (j = 0; j < E; ++j) {
+                    int32_t v = sr[j];
+                    if (j < m.nl[e]) v = 2 * m.lsym - v;
+                    else if (j >= m.nl[e] + ni[e]) v = 2 * m.rsym - v;
+                    ps[j] = v;
+                }
+                w->cnt[2 * k + e] = E;
+                w->nint[2 * k + e] = ni[e];
+            }
+        }
     }
     if (trace) {
         for (k = 0; k < K; ++k) {
@@ -214,14 +354,17 @@ static int64_t FN(mean_envelope_)(int64_t C, int64_t L, int64_t K, const REAL* c
             for (e = 0; e < 2; ++e) {
                 trace[2 * k + e].count = (int32_t)w->cnt[2 * k + e];
                 trace[2 * k + e].flags = 0;
-                trace[2 * k + e].hash = oracle_knot_hash(w->pos[e] + k * L, w->cnt[2 * k + e]);
+                trace[2 * k + e].hash = oracle_knot_hash(w->pos[e] + k * LS, w->cnt[2 * k + e]);
             }
         }
     }
     for (k = 0; k < K; ++k) {
         int64_t Em = w->cnt[2 * k], En = w->cnt[2 * k + 1];
         int64_t c;
-        if (!(Em > 3 && En > 3)) continue;
+        /* REF:840, 856: E_max > 3 && E_min > 3 with both end samples counted,
+         * i.e. at least two interior maxima and two interior minima (the same
+         * rule in the mirror mode, which then always finds its extrema) */
+        if (!(w->nint[2 * k] >= 2 && w->nint[2 * k + 1] >= 2)) continue;
         ++q;
 #pragma omp parallel for schedule(static) num_threads(w->nthreads)
         for (c = 0; c < C; ++c) {
@@ -231,12 +374,19 @@ static int64_t FN(mean_envelope_)(int64_t C, int64_t L, int64_t K, const REAL* c
 #ifdef _OPENMP
             tid = omp_get_thread_num();
 #endif
-            U = w->env + (size_t)tid * 9 * L;
-            Lo = U + L; vm = Lo + L; vn = vm + L; sws = vn + L;
-            FN(knot_values_)(w->pos[0] + k * L, Em, cur + c * L, 1, vm);
-            FN(knot_values_)(w->pos[1] + k * L, En, cur + c * L, 0, vn);
-            FN(envelope_)(w->pos[0] + k * L, vm, Em, L, U, sws);
-            FN(envelope_)(w->pos[1] + k * L, vn, En, L, Lo, sws);
+            U = w->env + (size_t)tid * 9 * LS;
+            Lo = U + LS; vm = Lo + LS; vn = vm + LS; sws = vn + LS;
+            if (!o->boundary) {
+                FN(knot_values_)(w->pos[0] + k * LS, Em, cur + c * L, 1, vm);
+                FN(knot_values_)(w->pos[1] + k * LS, En, cur + c * L, 0, vn);
+            } else {
+                const int32_t* sx = w->src[0] + k * LS;
+                const int32_t* sn = w->src[1] + k * LS;
+                for (n = 0; n < Em; ++n) vm[n] = cur[c * L + sx[n]];
+                for (n = 0; n < En; ++n) vn[n] = cur[c * L + sn[n]];
+            }
+            FN(envelope_)(w->pos[0] + k * LS, vm, Em, L, U, sws, o->spline_end);
+            FN(envelope_)(w->pos[1] + k * LS, vn, En, L, Lo, sws, o->spline_end);
             for (n = 0; n < L; ++n) {
                 /* REF:842 mean = (U + L) / 2.0, exact halving */
                 w->acc[c * L + n] = w->acc[c * L + n] + (U[n] + Lo[n]) * (REAL)0.5;
@@ -281,17 +431,22 @@ int FN(oracle_memd_)(int64_t C, int64_t L, int64_t K, int64_t nimf, int64_t max_
     memset(&w, 0, sizeof(w));
     w.nthreads = o.nthreads > 0 ? o.nthreads : 1;
     prows = K > C ? K : C;
-    w.pos[0] = (int32_t*)malloc(sizeof(int32_t) * (size_t)(K * L));
-    w.pos[1] = (int32_t*)malloc(sizeof(int32_t) * (size_t)(K * L));
+    w.pos[0] = (int32_t*)malloc(sizeof(int32_t) * (size_t)(K * (L + 4)));
+    w.pos[1] = (int32_t*)malloc(sizeof(int32_t) * (size_t)(K * (L + 4)));
+    w.src[0] = (int32_t*)malloc(sizeof(int32_t) * (size_t)(K * (L + 4)));
+    w.src[1] = (int32_t*)malloc(sizeof(int32_t) * (size_t)(K * (L + 4)));
     w.cnt = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * K));
+    w.nint = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * K));
     w.P = (REAL*)malloc(sizeof(REAL) * (size_t)(prows * L));
     w.acc = (REAL*)malloc(sizeof(REAL) * (size_t)(C * L));
     w.amp = (REAL*)malloc(sizeof(REAL) * (size_t)L);
-    w.env = (REAL*)malloc(sizeof(REAL) * (size_t)(9 * L) * (size_t)w.nthreads);
+    w.env = (REAL*)malloc(sizeof(REAL) * (size_t)(9 * (L + 4)) * (size_t)w.nthreads);
     cur = (REAL*)malloc(sizeof(REAL) * (size_t)(C * L));
     run = (REAL*)malloc(sizeof(REAL) * (size_t)(C * L));
-    if (!w.pos[0] || !w.pos[1] || !w.cnt || !w.P || !w.acc || !w.amp || !w.env || !cur || !run) {
-        free(w.pos[0]); free(w.pos[1]); free(w.cnt); free(w.P); free(w.acc); free(w.amp); free(w.env);
+    if (!w.pos[0] || !w.pos[1] || !w.src[0] || !w.src[1] || !w.cnt || !w.nint || !w.P || !w.acc || !w.amp ||
+        !w.env || !cur || !run) {
+        free(w.pos[0]); free(w.pos[1]); free(w.src[0]); free(w.src[1]); free(w.cnt); free(w.nint);
+        free(w.P); free(w.acc); free(w.amp); free(w.env);
         free(cur); free(run);
         return -2;
     }
@@ -328,7 +483,7 @@ int FN(oracle_memd_)(int64_t C, int64_t L, int64_t K, int64_t nimf, int64_t max_
                 if (nbit == 0) {
                     int64_t k, few = 1;
                     for (k = 0; k < K; ++k)
-                        if ((w.cnt[2 * k] - 2) + (w.cnt[2 * k + 1] - 2) >= 3) few = 0;
+                        if (w.nint[2 * k] + w.nint[2 * k + 1] >= 3) few = 0;
                     if (few) { imf_done = 1; break; }
                 }
                 if (q == 0) {
@@ -368,7 +523,8 @@ int FN(oracle_memd_)(int64_t C, int64_t L, int64_t K, int64_t nimf, int64_t max_
     for (j = i; j + 1 < nimf; ++j)
         for (n = 0; n < C * L; ++n) imfs[j * C * L + n] = 0;
     for (n = 0; n < C * L; ++n) imfs[(nimf - 1) * C * L + n] = run[n];   /* REF:1338 */
-    free(w.pos[0]); free(w.pos[1]); free(w.cnt); free(w.P); free(w.acc); free(w.amp); free(w.env);
+    free(w.pos[0]); free(w.pos[1]); free(w.src[0]); free(w.src[1]); free(w.cnt); free(w.nint);
+    free(w.P); free(w.acc); free(w.amp); free(w.env);
     free(cur); free(run);
     return 0;
 }

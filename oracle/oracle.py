@@ -26,6 +26,8 @@ class OracleOpts(ctypes.Structure):
         ("sd2", ctypes.c_double),
         ("tol", ctypes.c_double),
         ("nthreads", ctypes.c_int32),
+        ("spline_end", ctypes.c_int32),
+        ("boundary", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
     ]
 
@@ -60,8 +62,10 @@ def lib():
             g = getattr(L, "oracle_directions_" + sfx)
             g.argtypes = [i64, i64, vp, vp]
             g.restype = ctypes.c_int
-        L.oracle_envelope_f64.argtypes = [vp, vp, i64, i64, vp]
+        L.oracle_envelope_f64.argtypes = [vp, vp, i64, i64, vp, ctypes.c_int32]
         L.oracle_envelope_f64.restype = ctypes.c_int
+        L.oracle_mirror_f64.argtypes = [vp, i64, vp, i64, vp, i64, vp]
+        L.oracle_mirror_f64.restype = ctypes.c_int
         L.oracle_window_cover.argtypes = [i64]
         L.oracle_window_cover.restype = i64
         L.oracle_radical_inverse.argtypes = [ctypes.c_int32, ctypes.c_uint32]
@@ -104,19 +108,37 @@ def directions(C: int, K: int, primes=None, dtype=np.float64) -> np.ndarray:
     return out
 
 
-def envelope(pos, val, L: int) -> np.ndarray:
+def envelope(pos, val, L: int, nak: bool = False) -> np.ndarray:
+    """Spline through (pos, val) evaluated at 0..L-1; nak: not-a-knot ends."""
     p = np.ascontiguousarray(pos, dtype=np.int32)
     v = np.ascontiguousarray(val, dtype=np.float64)
     out = np.zeros(L, dtype=np.float64)
-    rc = lib().oracle_envelope_f64(_ptr(p), _ptr(v), p.size, L, _ptr(out))
+    rc = lib().oracle_envelope_f64(_ptr(p), _ptr(v), p.size, L, _ptr(out), int(nak))
     if rc != 0:
         raise RuntimeError(f"oracle_envelope failed rc={rc}")
     return out
 
 
+def mirror(P, imax, imin) -> dict:
+    """Mirrored end knots of one projection P with interior extrema imax, imin.
+    Returns lsym, rsym and per envelope (0 = maxima) the left / right source
+    samples in ascending order of mirrored position."""
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    a = np.ascontiguousarray(imax, dtype=np.int32)
+    b = np.ascontiguousarray(imin, dtype=np.int32)
+    out = np.zeros(22, dtype=np.int32)
+    rc = lib().oracle_mirror_f64(_ptr(P), P.size, _ptr(a), a.size, _ptr(b), b.size, _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_mirror failed rc={rc}")
+    nl, nr = out[2:4], out[4:6]
+    return {"lsym": int(out[0]), "rsym": int(out[1]),
+            "left": [list(out[6 + 4 * e: 6 + 4 * e + nl[e]]) for e in range(2)],
+            "right": [list(out[14 + 4 * e: 14 + 4 * e + nr[e]]) for e in range(2)]}
+
+
 def memd(y: np.ndarray, dirs: np.ndarray, num_imfs: int, max_iter: int, *,
          ref_window: bool = True, stop_mode: bool = False, sd=0.075, sd2=0.75, tol=0.075,
-         nthreads: int | None = None, trace: bool = False):
+         nthreads: int | None = None, trace: bool = False, spline_end: int = 0, boundary: int = 0):
     """Run the oracle.  y: C x L (channel-major), dirs: K x C.  Returns
     (imfs[num_imfs, C, L], info dict with sifts / n_imfs / trace)."""
     dtype = y.dtype
@@ -129,7 +151,7 @@ def memd(y: np.ndarray, dirs: np.ndarray, num_imfs: int, max_iter: int, *,
     assert dirs.shape == (K, C)
     imfs = np.zeros((num_imfs, C, L), dtype=dtype)
     o = OracleOpts(int(ref_window), int(stop_mode), sd, sd2, tol,
-                   nthreads if nthreads else max_threads(), 0)
+                   nthreads if nthreads else max_threads(), int(spline_end), int(boundary), 0)
     tr = np.zeros(num_imfs * (max_iter + 1) * K * 2, dtype=TRACE_DTYPE) if trace else None
     sifts = np.zeros(num_imfs, dtype=np.int32)
     nimf = np.zeros(1, dtype=np.int32)

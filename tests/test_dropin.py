@@ -75,6 +75,22 @@ def test_cli_matches_c_abi_and_oracle(tmp_path):
 
 
 @pytest.mark.gpu
+def test_cli_options_match_oracle(tmp_path):
+    y = mg.synth_eeg(3, 2000, 256.0, seed=8)
+    inp = str(tmp_path / "x.bin")
+    y.tofile(inp)
+    out = str(tmp_path / "imfs.bin")
+    r = subprocess.run([os.path.join(BIN, "memd_cli"), "--in", inp, "--channels", "3", "--f64", "--directions", "12",
+                        "--imfs", "4", "--iter", "4", "--spline", "nak", "--boundary", "mirror", "--out", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(out, dtype=np.float64).reshape(4, 3, 2000)
+    ref, _ = oracle.memd(y, oracle.directions(3, 12), 4, 4, spline_end=1, boundary=1)
+    for i in range(4):
+        assert np.linalg.norm(got[i] - ref[i]) / np.linalg.norm(ref[i]) < 1e-10
+
+
+@pytest.mark.gpu
 def test_mex_entry_matches_c_abi_with_mex_primes():
     torch = pytest.importorskip("torch")
     C, L, K, nimf, it = 6, 2500, 24, 5, 6

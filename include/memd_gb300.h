@@ -209,6 +209,16 @@ memd_status memd_run_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_
                                  const int64_t* offsets, const float* d_y, const float* d_dir,
                                  float* d_imfs, void* stream, memd_stats* stats);
 
+/* Batched run launched kernel by kernel without the graph, each kernel timed
+ * (per-stage figures, as memd_profile_*).  Synchronises the stream.
+ * memd_profile_batched_f32 takes mixed-form plans. */
+memd_status memd_profile_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
+                                     const int64_t* offsets, const double* d_y, const double* d_dir,
+                                     double* d_imfs, void* stream, memd_profile* prof);
+memd_status memd_profile_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
+                                     const int64_t* offsets, const float* d_y, const float* d_dir,
+                                     float* d_imfs, void* stream, memd_profile* prof);
+
 /* Direction set on the device.  primes == NULL: the standalone convention
  * (table {-K, 2, 3, 5, ...}); otherwise primes[0..C-1] (host memory) as the
  * MEX entry receives them.  d_dir: K x C. */

@@ -598,13 +598,12 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Pre
 // the working signal, run the decomposition graph over all of them at once,
 // and scatter the IMFs back to each epoch's block.
 template <int P>
-static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths, const int64_t* offsets,
-                                    const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
-                                    typename Prec<P>::T* d_imfs, void* stream, memd_stats* stats)
+static memd_status batched_inputs(memd_plan* p, int n, const int64_t* lengths, const int64_t* offsets,
+                                  const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
+                                  typename Prec<P>::T* d_imfs, cudaStream_t s)
 {
     using XT = typename Prec<P>::X;
     using T = typename Prec<P>::T;
-    cudaStream_t s = (cudaStream_t)stream;
     if (!p->batched) return set_error(MEMD_ERR_UNSUPPORTED, "run_batched: the plan was created without max_epochs");
     if (n < 1 || n > p->cfg.max_epochs) return set_error(MEMD_ERR_INVALID, "run_batched: n_epochs out of range");
     if (!lengths || !offsets || !d_y || !d_dir || !d_imfs) return set_error(MEMD_ERR_INVALID, "run_batched: null argument");
@@ -659,8 +658,6 @@ static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths,
     std::vector<long long> yoff(offsets, offsets + n);
     e = cudaMemcpyAsync(p->ep_yoff, yoff.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return set_cuda_error("run_batched: offsets", e);
-    memd_status st = build_graph<P>(p);
-    if (st != MEMD_OK) return st;
     cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
     // the gaps between epochs stay zero in every working buffer
     cudaMemsetAsync(p->run, 0, CL * sizeof(XT), s);
@@ -671,8 +668,24 @@ static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths,
     cudaMemcpyAsync(p->dir, d_dir, sizeof(T) * (size_t)g.K * C, cudaMemcpyDeviceToDevice, s);
     if constexpr (P == MEMD_PREC_MIXED)
         cudaMemsetAsync((float*)p->dir + (size_t)g.K * C, 0, sizeof(float) * (size_t)g.K * C, s);
+    return MEMD_OK;
+}
+
+template <int P>
+static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths, const int64_t* offsets,
+                                    const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
+                                    typename Prec<P>::T* d_imfs, void* stream, memd_stats* stats)
+{
+    using T = typename Prec<P>::T;
+    cudaStream_t s = (cudaStream_t)stream;
+    memd_status st = batched_inputs<P>(p, n, lengths, offsets, d_y, d_dir, d_imfs, s);
+    if (st != MEMD_OK) return st;
+    st = build_graph<P>(p);
+    if (st != MEMD_OK) return st;
+    const Geom& g = p->g;
+    const int C = g.C;
     cudaEventRecord(p->e0, s);
-    e = cudaGraphLaunch(p->exec, s);
+    cudaError_t e = cudaGraphLaunch(p->exec, s);
     if (e != cudaSuccess) return set_cuda_error("run_batched: graph launch", e);
     cudaEventRecord(p->e1, s);
     k_batched_out<T><<<1024, 256, 0, s>>>((const T*)p->imf, p->ep_yoff, d_imfs, C, g.L, (int)p->cfg.num_imfs, p->ep);
@@ -748,6 +761,35 @@ static memd_status profile_impl(memd_plan* p, const typename Prec<P>::T* d_y, co
     cudaEventDestroy(lc.a);
     cudaEventDestroy(lc.b);
     if (e != cudaSuccess) return set_cuda_error("profile: run", e);
+    return MEMD_OK;
+}
+
+// Batched run launched kernel by kernel, each timed (per-stage figures).
+template <int P>
+static memd_status profile_batched_impl(memd_plan* p, int n, const int64_t* lengths, const int64_t* offsets,
+                                        const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
+                                        typename Prec<P>::T* d_imfs, void* stream, memd_profile* prof)
+{
+    using T = typename Prec<P>::T;
+    cudaStream_t s = (cudaStream_t)stream;
+    memd_status st = batched_inputs<P>(p, n, lengths, offsets, d_y, d_dir, d_imfs, s);
+    if (st != MEMD_OK) return st;
+    memset(prof, 0, sizeof(*prof));
+    Launches lc;
+    lc.prof = prof;
+    lc.s = s;
+    cudaEventCreate(&lc.a);
+    cudaEventCreate(&lc.b);
+    memd_trace_entry* keep = p->trace_dev;
+    p->trace_dev = nullptr;
+    enqueue_decomposition<P>(p, s, lc);
+    p->trace_dev = keep;
+    k_batched_out<T><<<1024, 256, 0, s>>>((const T*)p->imf, p->ep_yoff, d_imfs, p->g.C, p->g.L,
+                                          (int)p->cfg.num_imfs, p->ep);
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaEventDestroy(lc.a);
+    cudaEventDestroy(lc.b);
+    if (e != cudaSuccess) return set_cuda_error("profile_batched: run", e);
     return MEMD_OK;
 }
 
@@ -864,7 +906,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         // halo lengths: the truncation error decays by <= 1/2 (solve) and
         // <= 1/3 (pivots) per knot; FP64 and double-float need ~1e-15
         const bool wide = f64 || c.precision == MEMD_PREC_MIXED;
-        p->S = 256;
+        p->S = 512;
         p->Ss = 64;
         p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : (wide ? 32 : 24));
         p->Sf = 64;
@@ -1076,6 +1118,28 @@ memd_status memd_profile_f32(memd_plan* plan, const float* d_y, const float* d_d
     if (plan->prec == MEMD_PREC_F32) return profile_impl<MEMD_PREC_F32>(plan, d_y, d_dir, d_imfs, stream, prof);
     if (plan->prec == MEMD_PREC_MIXED) return profile_impl<MEMD_PREC_MIXED>(plan, d_y, d_dir, d_imfs, stream, prof);
     return set_error(MEMD_ERR_PRECISION, "profile_f32: plan is FP64");
+}
+
+memd_status memd_profile_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
+                                     const int64_t* offsets, const double* d_y, const double* d_dir, double* d_imfs,
+                                     void* stream, memd_profile* prof)
+{
+    using namespace memd;
+    if (!plan || !prof) return set_error(MEMD_ERR_INVALID, "profile_batched: null argument");
+    if (plan->prec != MEMD_PREC_F64) return set_error(MEMD_ERR_PRECISION, "profile_batched_f64: plan is not FP64");
+    return profile_batched_impl<MEMD_PREC_F64>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream, prof);
+}
+
+memd_status memd_profile_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
+                                     const int64_t* offsets, const float* d_y, const float* d_dir, float* d_imfs,
+                                     void* stream, memd_profile* prof)
+{
+    using namespace memd;
+    if (!plan || !prof) return set_error(MEMD_ERR_INVALID, "profile_batched: null argument");
+    if (plan->prec == MEMD_PREC_MIXED)
+        return profile_batched_impl<MEMD_PREC_MIXED>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream,
+                                                     prof);
+    return set_error(MEMD_ERR_PRECISION, "profile_batched_f32: plan is not the mixed form");
 }
 
 memd_status memd_run_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths, const int64_t* offsets,

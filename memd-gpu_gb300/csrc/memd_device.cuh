@@ -136,11 +136,20 @@ template <> __device__ __forceinline__ float2 xfrom<float2>(float2 v) { return v
 // Channel-independent factorisation of the natural-spline system of one
 // (direction, envelope), per knot row i (Thomas elimination without pivoting):
 //   g_i = d_i - l_i * cp_{i-1};  m = 1/g_i;  lm = l_i/g_i;  cp = u_i/g_i;
-//   ih = 1 / (x_{i+1} - x_i)  (0 for the last row).
+//   ih = 1 / (x_{i+1} - x_i)  (0 for the last row); for the double-float
+//   form 3 / (x_{i+1} - x_i), the factor 3 of the right-hand side
+//   3 (slope_i - slope_{i-1}) folded in.
 template <typename real>
 struct alignas(4 * sizeof(real)) Fac {
     real m, lm, cp, ih;
 };
+template <typename real>
+constexpr bool kFacIh3 = false;
+template <>
+constexpr bool kFacIh3<dd> = true;
+__device__ __forceinline__ double fac_ih(double r) { return r; }
+__device__ __forceinline__ float fac_ih(float r) { return r; }
+__device__ __forceinline__ dd fac_ih(dd r) { return dd_mulf(r, 3.0f); }
 
 // Geometry of one record (or the widest epoch of a batch).
 struct Geom {

@@ -378,7 +378,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
                     o.m = wd ? mul_(m, div_(real(wn), real(wd))) : m;
                     o.lm = mul_(l, m);
                     o.cp = cp;
-                    o.ih = (i < E - 1) ? rtab[xr - xi] : real(0);
+                    o.ih = (i < E - 1) ? fac_ih(rtab[xr - xi]) : real(0);
                     f[i] = o;
                 }
                 xl = xi;
@@ -404,9 +404,10 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
 // window's truncated start perturbs the segment by at most that factor to the
 // power H; the rows a thread reads from the next segment are that segment's
 // own converged values, so the result does not depend on the segmentation.
-// H < 0 selects the exact single-window solve.  Segments hold S knots when
-// the system has more than 16 S knots, otherwise Ss (more, shorter segments
-// keep the GPU busy when the knot sets are short).  The segment index is the
+// H < 0 selects the exact single-window solve.  Segments hold the longest
+// power of two in [Ss, S] knots that leaves the system more than 16 segments
+// (more, shorter segments keep the GPU busy when the knot sets are short;
+// longer ones spend less on halos).  The segment index is the
 // slowest grid index, so whole CTAs past the active segments exit at once.
 // bnd != nullptr: raise bnd[c] (forward: max |y| over the segment's knots) and
 // bnd[C + c] (backward: max h^2 (|s_i| + |s_{i+1}|) / 4 over its pieces), float
@@ -435,7 +436,16 @@ __device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, i
     it.ok = false;
     it.E = cnt[it.env * g.K + k0 + it.kk];
     if (it.E > g.cap || it.E < 2) return it;
-    const int Se = (H < 0) ? g.cap : (it.E > 16 * S ? S : Ss);
+    // the longest power-of-two segment in [Ss, S] that still gives each
+    // system more than 16 segments
+    int Se = Ss;
+    if (H < 0) Se = g.cap;
+    else
+        for (int t = S; t > Ss; t >>= 1)
+            if (it.E > 16 * t) {
+                Se = t;
+                break;
+            }
     it.i0 = it.seg * Se;
     if (it.i0 >= it.E) return it;
     it.i1 = min(it.E, it.i0 + Se);
@@ -541,7 +551,10 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 const real ynext = yb[k];
                 real slope = real(0), r = real(0);
                 if (i < E - 1) slope = mul_(sub_(ynext, yi), ih);
-                if (!is_one(m)) r = mul_(real(3), sub_(slope, slope_prev));
+                if (!is_one(m)) {
+                    if constexpr (kFacIh3<real>) r = sub_(slope, slope_prev);  // slopes carry the factor 3
+                    else r = mul_(real(3), sub_(slope, slope_prev));
+                }
                 const real dcur = fmad_(-lm, dprev, mul_(m, r));
                 // rows before i0 only warm the recurrence up
                 if (i >= i0) {
@@ -609,8 +622,10 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
                 if (i < i1) {
                     if (cok && !(nak && i == E - 1)) o[(size_t)i * C] = sol;
                     if (bnd && i < E - 1) {
+                        // h^2 = 1 / ih^2 (9 / ih^2 when ih holds 3/h); the approximate
+                        // division's error is inside the 1.01 margin applied at the end
                         const float ih = magf(ihr);
-                        spart = fmaxf(spart, __fdiv_rn(0.25f * (magf(sol) + magf(snext)), ih * ih));
+                        spart = fmaxf(spart, __fdividef((kFacIh3<real> ? 2.25f : 0.25f) * (magf(sol) + magf(snext)), ih * ih));
                     }
                     if (nak && i == E - 3) {
                         const int hb = kn[E - 1] - kn[E - 2];

@@ -36,7 +36,8 @@ TRACE_DTYPE = np.dtype([("count", "<i4"), ("flags", "<i4"), ("hash", "<u8")])
 EXPORTS = [
     "memd_default_config", "memd_plan_create", "memd_plan_destroy", "memd_plan_workspace_bytes",
     "memd_plan_set_trace", "memd_run_f64", "memd_run_f32", "memd_run_batched_f64",
-    "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64", "memd_diag_fma_rate", "memd_last_error",
+    "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_profile_batched_f64",
+    "memd_profile_batched_f32", "memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64", "memd_diag_fma_rate", "memd_last_error",
     "memd_version", "memd_synth_tones", "memd_synth_eeg", "memd_write_bin", "memd_bin_count",
     "memd_read_bin",
 ]
@@ -126,6 +127,10 @@ def lib():
     for name in ("memd_profile_f64", "memd_profile_f32"):
         f = getattr(L, name)
         f.argtypes = [vp, vp, vp, vp, vp, ctypes.POINTER(Profile)]
+        f.restype = ctypes.c_int
+    for name in ("memd_profile_batched_f64", "memd_profile_batched_f32"):
+        f = getattr(L, name)
+        f.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Profile)]
         f.restype = ctypes.c_int
     for name in ("memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64"):
         f = getattr(L, name)
@@ -236,6 +241,17 @@ class Plan:
                   _dptr(dirs), _dptr(imfs), _stream_ptr(stream),
                   ctypes.byref(st) if stats else None))
         return st if stats else None
+
+    def profile_batched(self, y, lengths, offsets, dirs, imfs, stream=None) -> Profile:
+        """Batched run with every kernel timed by CUDA events (per-stage ms)."""
+        n = len(lengths)
+        la = (ctypes.c_int64 * n)(*[int(v) for v in lengths])
+        oa = (ctypes.c_int64 * n)(*[int(v) for v in offsets])
+        pr = Profile()
+        fn = lib().memd_profile_batched_f64 if self.cfg.precision == PREC_F64 else lib().memd_profile_batched_f32
+        _check(fn(self.handle, n, ctypes.cast(la, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p), _dptr(y),
+                  _dptr(dirs), _dptr(imfs), _stream_ptr(stream), ctypes.byref(pr)))
+        return pr
 
     def profile(self, y, dirs, imfs, stream=None) -> Profile:
         """Eager run with every kernel timed by CUDA events (per-stage ms)."""

@@ -102,3 +102,25 @@ def test_batched_api_misuse():
         plan.run_batched(y, [100, 100, 100], [0, 400, 800], d, out)
     assert ei.value.status == mg.MEMD_ERR_INVALID
     plan.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [mg.PREC_F64, mg.PREC_MIXED])
+def test_batched_profile_equals_graph_run(prec):
+    """The kernel-by-kernel profiled batched run computes what the graph does."""
+    torch = pytest.importorskip("torch")
+    C, nimf, it = 4, 3, 3
+    lengths = [700, 1500, 64]
+    recs, offs = _epochs(C, lengths, 77)
+    d = oracle.directions(C, 10)
+    tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
+    plan = mg.Plan(C, max(lengths), 10, nimf, it, precision=prec, max_epochs=len(lengths))
+    y = torch.as_tensor(np.concatenate([r.ravel() for r in recs]), dtype=tdt, device="cuda")
+    dd = torch.as_tensor(d, dtype=tdt, device="cuda")
+    a = torch.empty((nimf * y.numel(),), dtype=tdt, device="cuda")
+    b = torch.empty_like(a)
+    plan.run_batched(y, lengths, offs, dd, a)
+    pr = plan.profile_batched(y, lengths, offs, dd, b).as_dict()
+    plan.close()
+    assert torch.equal(a, b)
+    assert pr["solve"]["launches"] == 2 * (nimf - 1) * it and pr["eval"]["ms"] > 0

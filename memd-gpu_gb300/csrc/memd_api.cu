@@ -909,8 +909,8 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         p->S = 512;
         p->Ss = 64;
         p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : (wide ? 32 : 24));
-        p->Sf = 64;
-        p->Hf = wide ? 40 : 20;
+        p->Sf = 16;  // short factorisation segments: the pivot recurrence is latency-bound
+        p->Hf = f64 ? 40 : (wide ? 32 : 20);
     }
     p->GS = 32;  // solve: one warp per (envelope, direction, segment, 32 channels)
     p->ngroups = (C + 31) / 32;

@@ -298,7 +298,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
     // 32 m <= 2 h, h the chunk's mean knot spacing, so that rounding carried
     // across a span grows by at most ~(32m/h)^2 = 4 over a direct evaluation;
     // at the densest knots m = 1), and splits each span's (direction,
-    // envelope) pairs over P = m CTAs
+    // envelope) pairs over P <= m CTAs
     if (cumcfg && blockIdx.x == 0 && threadIdx.x < 32) {
         int q = 0;
         long long et = 0;
@@ -317,8 +317,15 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
                 const double h = (double)g.L * (2.0 * q) / (double)et;
                 while (m < 8 && 32.0 * (2 * m) <= 2.0 * h) m *= 2;
             }
+            // parts per span: the fewest (a power of two <= m) that still give
+            // the launch ~2048 working CTAs; a long record or a batch has
+            // enough spans on its own, and every extra part costs a flush of
+            // the span's accumulators
+            const long spans = (long)((g.W + m - 1) / m) * ((g.C + 31) / 32);
+            int P = m;
+            while (P > 1 && spans * (P / 2) >= 2048) P >>= 1;
             cumcfg[0] = m;
-            cumcfg[1] = m;
+            cumcfg[1] = P;
         }
     }
     const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1234,7 +1241,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const int C = g.C;
     const int mw = min(max(cumcfg[0], 1), kCumMaxWords), P = min(max(cumcfg[1], 1), kCumMaxParts);
     // CTA b works on part b % P of span b / P (launched: W rounded up to a
-    // multiple of 8 CTAs, so that every part of every span exists; P = m | 8)
+    // multiple of 8 CTAs, so that every part of every span exists; P | m | 8)
     const int si = blockIdx.x / P, prt = blockIdx.x % P;
     const int w = si * mw;
     if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)

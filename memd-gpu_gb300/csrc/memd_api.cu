@@ -96,6 +96,7 @@ struct memd_plan {
     int* knots;
     int* cnt;
     int* mir;       // mirror boundary: [K][kMirWords] mirrored end knots per direction
+    memd::CompactShared csh;  // chunked compaction: per-chunk counts, hash sums, arrival counters
     RunState* st;
     int* coord_bad;
     int* host_flag;
@@ -303,10 +304,16 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
                                                               nullptr, p->mir, g, k0, kc);
             lc.end(MEMD_STAGE_PROJECT);
         }
+        const int nch = (g.W + kCompactChunk - 1) / kCompactChunk;
+        if (nch > 1) {
+            lc.begin();
+            k_compact_count<<<dim3((unsigned)nch, (unsigned)(2 * kc)), 512, 0, s>>>(p->bits, p->csh.ctot, g, nch);
+            lc.end(MEMD_STAGE_COMPACT);
+        }
         lc.begin();
-        k_compact<R, XT><<<(unsigned)(2 * kc), 512, 0, s>>>(p->bits, p->wpref, p->knots, p->cnt, (R*)p->yv,
-                                                            (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows,
-                                                            p->cum ? (R*)p->yend : nullptr, p->ep, p->mir);
+        k_compact<R, XT><<<dim3((unsigned)nch, (unsigned)(2 * kc)), 512, 0, s>>>(
+            p->bits, p->wpref, p->knots, p->cnt, (R*)p->yv, (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows,
+            p->cum ? (R*)p->yend : nullptr, p->ep, p->mir, p->csh, nch);
         lc.end(MEMD_STAGE_COMPACT);
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
@@ -909,7 +916,9 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         p->S = 512;
         p->Ss = 64;
         p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : (wide ? 32 : 24));
-        p->Sf = 16;  // short factorisation segments: the pivot recurrence is latency-bound
+        // short factorisation segments (the pivot recurrence is latency-bound),
+        // except for FP64, whose longer halo would dominate
+        p->Sf = f64 ? 64 : 16;
         p->Hf = f64 ? 40 : (wide ? 32 : 20);
     }
     p->GS = 32;  // solve: one warp per (envelope, direction, segment, 32 channels)
@@ -979,6 +988,10 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     ALLOC(p->knots, sizeof(int) * 2 * Kc * p->g.cap);
     ALLOC(p->cnt, sizeof(int) * 2 * (size_t)K);
     if (p->g.mirror) ALLOC(p->mir, sizeof(int) * kMirWords * (size_t)K);
+    const size_t nch_max = (size_t)(p->g.W + kCompactChunk - 1) / kCompactChunk;
+    ALLOC(p->csh.ctot, sizeof(int) * 2 * Kc * nch_max);
+    ALLOC(p->csh.hacc, sizeof(unsigned long long) * 2 * Kc);
+    ALLOC(p->csh.arrive, sizeof(int) * 2 * Kc);
     ALLOC(p->fac, rb * 4 * 2 * Kc * p->g.cap);
     if (!p->cum) ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
     else ALLOC(p->yend, rb * 2 * Kc * (size_t)std::max<int64_t>(1, c.max_epochs) * 2 * C);  // [2][Kc][epochs][2][C]
@@ -1039,6 +1052,8 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         cudaFree(r32);
         cudaFree(rdd);
     }
+    if (e == cudaSuccess) e = cudaMemset(p->csh.hacc, 0, sizeof(unsigned long long) * 2 * (size_t)p->Kc);
+    if (e == cudaSuccess) e = cudaMemset(p->csh.arrive, 0, sizeof(int) * 2 * (size_t)p->Kc);
     if (e == cudaSuccess && p->cum) {
         e = cudaMemset(p->cumsh.kq, 0, sizeof(unsigned long long) * 35 * (size_t)p->g.W * C);
         if (e == cudaSuccess) e = cudaMemset(p->cumsh.anc, 0, sizeof(unsigned long long) * 4 * (size_t)p->g.W * C);

@@ -120,45 +120,84 @@ k_project_extrema(const XT* __restrict__ X, const real* __restrict__ dir,
     }
 }
 
+// Knot lists.  The bitmask of each (envelope, direction) is cut into chunks of
+// kCompactChunk words; CTA (chunk, slot) of 512 threads writes the knots of its
+// chunk (each thread an ordered run of words, a block scan of the popcounts,
+// the offset of the chunk from k_compact_count's per-chunk totals) and gathers
+// their values; the last CTA of a slot to arrive (an atomic counter, no
+// waiting) writes the count, the trace entry, the mirrored knots and the
+// end-point clamp.  A record of up to kCompactChunk words is one chunk and
+// needs no count pass.
 // ---------------------------------------------------------------------------
-// Knot lists.  One CTA of 512 threads per (envelope, direction).
-// ---------------------------------------------------------------------------
+constexpr int kCompactChunk = 4096;
+
+struct CompactShared {
+    int* ctot;                 // [2 Kc][nch] interior knots per chunk
+    unsigned long long* hacc;  // [2 Kc] trace hash partial sums (zero between launches)
+    int* arrive;               // [2 Kc] CTAs done (zero between launches)
+};
+
+__global__ void __launch_bounds__(512)
+k_compact_count(const uint32_t* __restrict__ bits, int* __restrict__ ctot, Geom g, int nch)
+{
+    const int chunk = blockIdx.x, slot = blockIdx.y;
+    const uint32_t* b = bits + (size_t)slot * g.W;
+    const int w0 = chunk * kCompactChunk, w1 = min(g.W, w0 + kCompactChunk);
+    int local = 0;
+    for (int w = w0 + (int)threadIdx.x; w < w1; w += blockDim.x) local += __popc(b[w]);
+    local = warp_sum(local);
+    __shared__ int ws[16];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) ws[wid] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += ws[i];
+        ctot[(size_t)slot * nch + chunk] = t;
+    }
+}
+
 template <typename real, typename XT>
 __global__ void __launch_bounds__(512)
 k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __restrict__ knots,
           int* __restrict__ cnt, real* __restrict__ yv, const XT* __restrict__ X,
           memd_trace_entry* __restrict__ trace, Geom g, int k0, int Kc, RunState* st, int trace_rows,
-          real* __restrict__ yend, Epochs ep, const int* __restrict__ mir)
+          real* __restrict__ yend, Epochs ep, const int* __restrict__ mir, CompactShared cs, int nch)
 {
-    // g.mirror: the knot list is [left mirrored | interior extrema | right
-    // mirrored] (mir from k_mirror); wpref and the bitmask count the interior
-    // extrema only, the knot values come from the mirrored knots' source
-    // samples, and the reference's end-point clamp does not apply.
     // yend != nullptr: the knot values are not gathered; only the two end
     // knots' values (clamped) are written, to yend[env][kk][2][C], and the
     // consumers read the interior knot values from X.
     // trace_rows > 0: trace is the base of a [trace_rows][K][2] array and the
     // row of this pass is st->trace_row (stop mode); otherwise trace points at
     // this pass's [K][2] block.
-    if (trace && trace_rows > 0) {
-        const int r = st->trace_row;
-        trace = (r >= 0 && r < trace_rows) ? trace + (size_t)r * g.K * 2 : nullptr;
-    }
-    const int env = blockIdx.x / Kc, kk = blockIdx.x - env * Kc;
-    const size_t slot = (size_t)env * Kc + kk;
+    // g.mirror: the knot list is [left mirrored | interior extrema | right
+    // mirrored] (mir from k_mirror); wpref and the bitmask count the interior
+    // extrema only, the knot values come from the mirrored knots' source
+    // samples, and the reference's end-point clamp does not apply.
+    const int chunk = blockIdx.x;
+    const int slot_i = blockIdx.y;
+    const int env = slot_i / Kc, kk = slot_i - env * Kc;
+    const size_t slot = (size_t)slot_i;
     const uint32_t* b = bits + slot * g.W;
     int* wp = wpref + slot * (g.W + 1);
     int* kn = knots + slot * g.cap;
     const int* mi = g.mirror ? mir + (size_t)(k0 + kk) * kMirWords : nullptr;
     const int nlm = mi ? mi[kMirNl + env] : 0, nrm = mi ? mi[kMirNr + env] : 0;
-    const int per = (g.W + blockDim.x - 1) / blockDim.x;
-    const int wb = threadIdx.x * per, we = min(g.W, wb + per);
-    int local = 0;
-    for (int w = wb; w < we; ++w) local += __popc(b[w]);
+    const int C = g.C;
     __shared__ int wsum[16];
     __shared__ unsigned long long hsum[16];
-    __shared__ int total_s;
+    __shared__ int total_s, off_s, last_s;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        int o = 0;
+        for (int c = 0; c < chunk; ++c) o += cs.ctot[slot * nch + c];
+        off_s = o;
+    }
+    const int cw0 = chunk * kCompactChunk, cw1 = min(g.W, cw0 + kCompactChunk);
+    const int per = (cw1 - cw0 + blockDim.x - 1) / blockDim.x;
+    const int wb = cw0 + threadIdx.x * per, we = min(cw1, wb + per);
+    int local = 0;
+    for (int w = wb; w < we; ++w) local += __popc(b[w]);
     int incl = local;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -180,7 +219,8 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
         if (lane == nw - 1) total_s = iv;
     }
     __syncthreads();
-    int run = wsum[wid] + incl - local;
+    const int off = off_s;
+    int run = off + wsum[wid] + incl - local;
     uint64_t h = 0;
     for (int w = wb; w < we; ++w) {
         wp[w] = run;
@@ -194,79 +234,121 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
             h += splitmix64((uint64_t)(uint32_t)n);
         }
     }
-    const int Eint = total_s;
-    const int E = nlm + Eint + nrm;
     h = warp_sum<unsigned long long>(h);
     if (lane == 0) hsum[wid] = h;
+    __syncthreads();
+    // values of this chunk's interior knots, every channel (contiguous per knot)
+    if (!yend) {
+        real* y = yv + slot * (size_t)g.cap * C;
+        const int i0 = nlm + off, i1 = min(g.cap, nlm + off + total_s);
+        for (int idx = threadIdx.x; idx < (i1 - i0) * C; idx += blockDim.x) {
+            const int i = i0 + idx / C, c = idx % C;
+            y[(size_t)i * C + c] = xval<real>(X[(size_t)kn[i] * C + c]);
+        }
+    }
+    unsigned long long hchunk = 0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) hchunk += hsum[i];
+    // the last CTA of the slot finishes it
+    if (nch > 1) {
+        if (threadIdx.x == 0) atomicAdd(&cs.hacc[slot], hchunk);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) last_s = (atomicAdd(&cs.arrive[slot], 1) == nch - 1);
+        __syncthreads();
+        if (!last_s) return;  // uniform over the CTA
+        __threadfence();
+    }
+    // from here on, knots and prefix counts written by the slot's other CTAs
+    // are read through L2 (__ldcg): this CTA's L1 may hold lines it read earlier
     if (threadIdx.x == 0) {
+        int Eint = total_s;
+        if (nch > 1) {
+            Eint = 0;
+            for (int c = 0; c < nch; ++c) Eint += __ldcg(&cs.ctot[slot * nch + c]);
+        }
+        unsigned long long htot = hchunk;
+        if (nch > 1) {
+            htot = __ldcg(&cs.hacc[slot]);
+            cs.hacc[slot] = 0ull;
+            cs.arrive[slot] = 0;
+        }
+        const int E = nlm + Eint + nrm;
         wp[g.W] = Eint;
         cnt[env * g.K + k0 + kk] = E;
         if (E > g.cap) atomicOr(&st->flags, 2);
+        // mirrored knots: positions, and their part of the trace hash
+        if (mi) {
+            for (int j = 0; j < nlm; ++j) {
+                const int pos = 2 * mi[kMirLsym] - mi[kMirLsrc + 2 * env + j];
+                if (j < g.cap) kn[j] = pos;
+                htot += splitmix64((uint64_t)(uint32_t)pos);
+            }
+            for (int j = 0; j < nrm; ++j) {
+                const int pos = 2 * mi[kMirRsym] - mi[kMirRsrc + 2 * env + j];
+                if (nlm + Eint + j < g.cap) kn[nlm + Eint + j] = pos;
+                htot += splitmix64((uint64_t)(uint32_t)pos);
+            }
+        }
+        memd_trace_entry* tr = trace;
+        if (tr && trace_rows > 0) {
+            const int r = st->trace_row;
+            tr = (r >= 0 && r < trace_rows) ? tr + (size_t)r * g.K * 2 : nullptr;
+        }
+        if (tr) {
+            memd_trace_entry e;
+            e.count = E;
+            e.flags = 0;
+            e.hash = htot;
+            tr[(size_t)(k0 + kk) * 2 + env] = e;
+        }
+        total_s = E;
+        off_s = Eint;
     }
     __syncthreads();
-    unsigned long long hm = 0;  // hash of the mirrored knots
-    if (mi && threadIdx.x == 0) {
-        for (int j = 0; j < nlm; ++j) {
-            const int pos = 2 * mi[kMirLsym] - mi[kMirLsrc + 2 * env + j];
-            if (j < g.cap) kn[j] = pos;
-            hm += splitmix64((uint64_t)(uint32_t)pos);
-        }
-        for (int j = 0; j < nrm; ++j) {
-            const int pos = 2 * mi[kMirRsym] - mi[kMirRsrc + 2 * env + j];
-            if (nlm + Eint + j < g.cap) kn[nlm + Eint + j] = pos;
-            hm += splitmix64((uint64_t)(uint32_t)pos);
-        }
-    }
-    if (trace && threadIdx.x == 0) {
-        unsigned long long t = hm;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += hsum[i];
-        memd_trace_entry e;
-        e.count = E;
-        e.flags = 0;
-        e.hash = t;
-        trace[(size_t)(k0 + kk) * 2 + env] = e;
-    }
+    const int E = total_s, Eint = off_s;
     if (E > g.cap || E < 2) return;
-    // Knot values of every channel (contiguous per knot), then the end-point
-    // clamp of the two end knots of each record (REF:447-486 max, 545-584 min).
-    const int C = g.C;
     const int nrec = ep.n > 0 ? ep.n : 1;
     if (ep.n > 0) {
         for (int e = threadIdx.x; e < ep.n; e += blockDim.x)
-            ep.cnt[((size_t)env * g.K + k0 + kk) * ep.n + e] = wp[ep.w0[e + 1]] - wp[ep.w0[e]];
+            ep.cnt[((size_t)env * g.K + k0 + kk) * ep.n + e] = __ldcg(&wp[ep.w0[e + 1]]) - __ldcg(&wp[ep.w0[e]]);
     }
-    if (!yend) {
-        real* y = yv + slot * (size_t)g.cap * C;
-        for (int idx = threadIdx.x; idx < E * C; idx += blockDim.x) {
-            const int i = idx / C, c = idx - i * C;
-            int src;
-            if (!mi) src = kn[i];
-            else if (i < nlm) src = mi[kMirLsrc + 2 * env + i];
-            else if (i >= nlm + Eint) src = mi[kMirRsrc + 2 * env + (i - nlm - Eint)];
-            else src = kn[i];
-            y[idx] = xval<real>(X[(size_t)src * C + c]);
+    if (mi) {
+        // the mirrored knots' values from their source samples
+        if (!yend) {
+            real* y = yv + slot * (size_t)g.cap * C;
+            for (int idx = threadIdx.x; idx < (nlm + nrm) * C; idx += blockDim.x) {
+                const int j = idx / C, c = idx % C;
+                const int i = j < nlm ? j : nlm + Eint + (j - nlm);
+                const int src = j < nlm ? mi[kMirLsrc + 2 * env + j] : mi[kMirRsrc + 2 * env + (j - nlm)];
+                y[(size_t)i * C + c] = xval<real>(X[(size_t)src * C + c]);
+            }
         }
-        __syncthreads();  // the raw end values are written before the clamped ones replace them
+        return;
     }
-    if (mi) return;
+    // The end-point clamp of the two end knots of each record (REF:447-486
+    // max, 545-584 min); the raw end values were gathered with the chunks.
     for (int idx = threadIdx.x; idx < nrec * C; idx += blockDim.x) {
         const int e = idx / C, c = idx - e * C;
-        const int kb = ep.n > 0 ? wp[ep.w0[e]] : 0;
-        const int ke = ep.n > 0 ? wp[ep.w0[e + 1]] : E;  // the record's knots: kb .. ke - 1
+        const int kb = ep.n > 0 ? __ldcg(&wp[ep.w0[e]]) : 0;
+        const int ke = ep.n > 0 ? __ldcg(&wp[ep.w0[e + 1]]) : E;  // the record's knots: kb .. ke - 1
         const int Er = ke - kb;
         const int* kr = kn + kb;
-        real v0 = xval<real>(X[(size_t)kr[0] * C + c]);
-        real vE = xval<real>(X[(size_t)kr[Er - 1] * C + c]);
+        const int x0 = __ldcg(&kr[0]), xE = __ldcg(&kr[Er - 1]);
+        real v0 = xval<real>(X[(size_t)x0 * C + c]);
+        real vE = xval<real>(X[(size_t)xE * C + c]);
         if (Er - 1 > 4) {
-            const real v1 = xval<real>(X[(size_t)kr[1] * C + c]);
-            const real v2 = xval<real>(X[(size_t)kr[2] * C + c]);
-            real slope = div_(sub_(v2, v1), real(kr[2] - kr[1]));
-            real t = fmad_(-slope, real(kr[1] - kr[0]), v1);
+            const int x1 = __ldcg(&kr[1]), x2 = __ldcg(&kr[2]);
+            const int xa = __ldcg(&kr[Er - 3]), xb = __ldcg(&kr[Er - 2]);
+            const real v1 = xval<real>(X[(size_t)x1 * C + c]);
+            const real v2 = xval<real>(X[(size_t)x2 * C + c]);
+            real slope = div_(sub_(v2, v1), real(x2 - x1));
+            real t = fmad_(-slope, real(x1 - x0), v1);
             if (env == 0 ? (t > v0) : (t < v0)) v0 = t;
-            const real a = xval<real>(X[(size_t)kr[Er - 3] * C + c]);
-            const real bb = xval<real>(X[(size_t)kr[Er - 2] * C + c]);
-            slope = div_(sub_(bb, a), real(kr[Er - 2] - kr[Er - 3]));
-            t = fmad_(slope, real(kr[Er - 1] - kr[Er - 2]), bb);
+            const real a = xval<real>(X[(size_t)xa * C + c]);
+            const real bb = xval<real>(X[(size_t)xb * C + c]);
+            slope = div_(sub_(bb, a), real(xb - xa));
+            t = fmad_(slope, real(xE - xb), bb);
             if (env == 0 ? (t > vE) : (t < vE)) vE = t;
         }
         if (yend) {

@@ -328,27 +328,33 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         unsigned* bcur = p->cum ? p->bnd + (size_t)(p->bpass & 1) * 2 * g.C : nullptr;
         lc.begin();
         bool xm = false;
+#define MEMD_FWD(XM_, EPB_, NAK_)                                                                               \
+    k_solve_fwd<R, XT, XM_, EPB_, NAK_><<<nb, kSolveThreads, 0, s>>>(                                          \
+        (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, \
+        bcur, XM_ ? (const XT*)p->X : nullptr, p->knots, XM_ ? (const R*)p->yend : nullptr, p->ep)
         if constexpr (P == MEMD_PREC_MIXED) {
             if (p->cum) {  // knot values from the working signal (the impulse-accumulation path)
                 xm = true;
-                if (p->ep.n == 0)
-                    k_solve_fwd<R, XT, true, false><<<nb, kSolveThreads, 0, s>>>(
-                        (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H,
-                        p->ngroups, bcur, (const XT*)p->X, p->knots, (const R*)p->yend, p->ep);
-                else
-                    k_solve_fwd<R, XT, true, true><<<nb, kSolveThreads, 0, s>>>(
-                        (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H,
-                        p->ngroups, bcur, (const XT*)p->X, p->knots, (const R*)p->yend, p->ep);
+                if (p->ep.n > 0) MEMD_FWD(true, true, false);  // batched runs: natural ends only
+                else if (g.nak) MEMD_FWD(true, false, true);
+                else MEMD_FWD(true, false, false);
             }
         }
-        if (!xm)
-            k_solve_fwd<R, XT, false, false><<<nb, kSolveThreads, 0, s>>>(
-                (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H, p->ngroups,
-                bcur, nullptr, p->knots, nullptr, p->ep);
+        if (!xm) {
+            if (g.nak) MEMD_FWD(false, false, true);
+            else MEMD_FWD(false, false, false);
+        }
+#undef MEMD_FWD
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
-        k_solve_bwd<R><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0,
-                                                   kc, p->S, p->Ss, p->H, p->ngroups, bcur, p->knots);
+        if (g.nak)
+            k_solve_bwd<R, true><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
+                                                             (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
+                                                             p->knots);
+        else
+            k_solve_bwd<R, false><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
+                                                              (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
+                                                              p->knots);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin();
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
@@ -913,7 +919,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         // halo lengths: the truncation error decays by <= 1/2 (solve) and
         // <= 1/3 (pivots) per knot; FP64 and double-float need ~1e-15
         const bool wide = f64 || c.precision == MEMD_PREC_MIXED;
-        p->S = 512;
+        p->S = 256;
         p->Ss = 64;
         p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : (wide ? 32 : 24));
         // short factorisation segments (the pivot recurrence is latency-bound),

@@ -542,7 +542,7 @@ __device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, i
     return it;
 }
 
-template <typename real, typename XT, bool XM, bool EPB>
+template <typename real, typename XT, bool XM, bool EPB, bool NAK>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
             real* __restrict__ dbuf, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
@@ -640,7 +640,9 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 const real ynext = yb[k];
                 real slope = real(0), r = real(0);
                 if (i < E - 1) slope = mul_(sub_(ynext, yi), ih);
-                if (!is_one(m)) {
+                // identity rows (record ends) have lm = 0 and m = 1; a not-a-knot
+                // row 1 also has lm = 0, so NAK tells them apart by m
+                if (NAK ? !is_one(m) : !is_zero(lm)) {
                     if constexpr (kFacIh3<real>) r = sub_(slope, slope_prev);  // slopes carry the factor 3
                     else r = mul_(real(3), sub_(slope, slope_prev));
                 }
@@ -662,13 +664,13 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     }
 }
 
-template <typename real>
+template <typename real, bool NAK>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, const real* __restrict__ dbuf,
             real* __restrict__ sv, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
             unsigned* __restrict__ bnd, const int* __restrict__ knots)
 {
-    // Not-a-knot end conditions (g.nak, E >= 4): rows 0 and E-1 were solved as
+    // NAK (not-a-knot end conditions, g.nak), E >= 4: rows 0 and E-1 were solved as
     // identity rows; s_0 = s_1 + (h_0 / h_1)(s_1 - s_2) is applied at row 0,
     // and s_{E-1} = s_{E-2} + (h_{E-2} / h_{E-3})(s_{E-2} - s_{E-3}) by the
     // warp that owns row E-3 (its window always reaches row E-1, and row E-2
@@ -685,7 +687,7 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     const real* d = dbuf + slot * (size_t)g.cap * C + cl;
     real* o = sv + slot * (size_t)g.cap * C + cl;
     const int* kn = knots + slot * g.cap;
-    const bool nak = g.nak && E >= 4;
+    const bool nak = NAK && E >= 4;
     const int ie = (H < 0) ? E : min(E, i1 + H);
     real snext = real(0), snext2 = real(0);
     float spart = 0.0f;
@@ -706,24 +708,29 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
             if (k < nb) {
                 const int i = top - k;
                 real sol = fmad_(-cp, snext, db[k]);
-                if (nak && i == 0)
-                    sol = add_(snext, div_(mul_(sub_(snext, snext2), real(kn[1] - kn[0])), real(kn[2] - kn[1])));
+                if constexpr (NAK) {
+                    if (nak && i == 0)
+                        sol = add_(snext, div_(mul_(sub_(snext, snext2), real(kn[1] - kn[0])), real(kn[2] - kn[1])));
+                }
                 if (i < i1) {
-                    if (cok && !(nak && i == E - 1)) o[(size_t)i * C] = sol;
+                    if (cok && !(NAK && nak && i == E - 1)) o[(size_t)i * C] = sol;
                     if (bnd && i < E - 1) {
                         // h^2 = 1 / ih^2 (9 / ih^2 when ih holds 3/h); the approximate
                         // division's error is inside the 1.01 margin applied at the end
                         const float ih = magf(ihr);
                         spart = fmaxf(spart, __fdividef((kFacIh3<real> ? 2.25f : 0.25f) * (magf(sol) + magf(snext)), ih * ih));
                     }
-                    if (nak && i == E - 3) {
-                        const int hb = kn[E - 1] - kn[E - 2];
-                        const real sl = add_(snext, div_(mul_(sub_(snext, sol), real(hb)), real(kn[E - 2] - kn[E - 3])));
-                        if (cok) o[(size_t)(E - 1) * C] = sl;
-                        if (bnd) spart = fmaxf(spart, 0.25f * (magf(snext) + magf(sl)) * (float)hb * (float)hb);
+                    if constexpr (NAK) {
+                        if (nak && i == E - 3) {
+                            const int hb = kn[E - 1] - kn[E - 2];
+                            const real sl =
+                                add_(snext, div_(mul_(sub_(snext, sol), real(hb)), real(kn[E - 2] - kn[E - 3])));
+                            if (cok) o[(size_t)(E - 1) * C] = sl;
+                            if (bnd) spart = fmaxf(spart, 0.25f * (magf(snext) + magf(sl)) * (float)hb * (float)hb);
+                        }
                     }
                 }
-                snext2 = snext;
+                if constexpr (NAK) snext2 = snext;
                 snext = sol;
             }
         }

@@ -1434,43 +1434,49 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
                 aD = aD + d;
             }
             // (3) jumps q_j - q_{j-1} at row x_j - p0 (in 1 .. nl + 2), q_j the
-            //     quantised d_j = (s_{j+1} - s_j) / (3 h_j); batches of KB knots
+            //     quantised d_j = (s_{j+1} - s_j) / (3 h_j); full batches of KB
+            //     knots (loads first, no predication), then the remainder
             const int j0 = eJ[le];
             if (n > 0) {
                 int xj = kn[j0];
                 dd sj = sv[rb + (size_t)j0 * C];
                 unsigned long long qprev = qfix((sj - sv[rb + (size_t)(j0 - 1) * C]) * rtab3[xj - kn[j0 - 1]], sh);
-                for (int t0 = 0; t0 < n; t0 += KB) {
-                    const int nb = min(KB, n - t0);
+                int t0 = 0;
+                for (; t0 + KB <= n; t0 += KB) {
                     int xn[KB];
                     dd sn[KB], r3[KB];
+                    const int* knp = kn + j0 + t0 + 1;
+                    const dd* svp = sv + rb + (size_t)(j0 + t0 + 1) * C;
 #pragma unroll
                     for (int k = 0; k < KB; ++k) {
-                        if (k < nb) {
-                            xn[k] = kn[j0 + t0 + k + 1];
-                            sn[k] = sv[rb + (size_t)(j0 + t0 + k + 1) * C];
-                        }
+                        xn[k] = knp[k];
+                        sn[k] = svp[(size_t)k * C];
                     }
                     {
                         int xa = xj;
 #pragma unroll
                         for (int k = 0; k < KB; ++k) {
-                            if (k < nb) {
-                                r3[k] = rtab3[xn[k] - xa];
-                                xa = xn[k];
-                            }
+                            r3[k] = rtab3[xn[k] - xa];
+                            xa = xn[k];
                         }
                     }
 #pragma unroll
                     for (int k = 0; k < KB; ++k) {
-                        if (k < nb) {
-                            const unsigned long long qcur = qfix((sn[k] - sj) * r3[k], sh);
-                            atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
-                            qprev = qcur;
-                            xj = xn[k];
-                            sj = sn[k];
-                        }
+                        const unsigned long long qcur = qfix((sn[k] - sj) * r3[k], sh);
+                        atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
+                        qprev = qcur;
+                        xj = xn[k];
+                        sj = sn[k];
                     }
+                }
+                for (; t0 < n; ++t0) {
+                    const int xn1 = kn[j0 + t0 + 1];
+                    const dd sn1 = sv[rb + (size_t)(j0 + t0 + 1) * C];
+                    const unsigned long long qcur = qfix((sn1 - sj) * rtab3[xn1 - xj], sh);
+                    atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
+                    qprev = qcur;
+                    xj = xn1;
+                    sj = sn1;
                 }
             }
         }

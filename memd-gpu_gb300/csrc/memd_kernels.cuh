@@ -600,8 +600,11 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     if (is > 0) slope_prev = mul_(sub_(yi, yrow(is - 1)), f[is - 1].ih);
     real dprev = real(0);
     float ymax = 0.0f;
-    for (int base = is; base < i1; base += B) {
-        const int nb = min(B, i1 - base);
+    // one batch of B rows; FULL (a compile-time flag): all B rows are owned
+    // (>= i0), below i1 and have a right neighbour, so no row needs a guard
+    auto batch = [&](auto full, int base) {
+        constexpr bool FULL = decltype(full)::value;
+        const int nb = FULL ? B : min(B, i1 - base);
         real fm = real(0), flm = real(0), fih = real(0);
         int fx = 0, ffl = 0, fe = 0;
         if (lane < nb) {
@@ -626,20 +629,21 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 } else {
                     fl = endfl(base + 1 + k, n, e);
                 }
-                yb[k] = (k < nb && base + 1 + k < E) ? yx(n, fl, e) : real(0);
+                yb[k] = (FULL || (k < nb && base + 1 + k < E)) ? yx(n, fl, e) : real(0);
             }
         } else {
 #pragma unroll
-            for (int k = 0; k < B; ++k) yb[k] = (k < nb && base + 1 + k < E) ? y[(size_t)(base + 1 + k) * C] : real(0);
+            for (int k = 0; k < B; ++k)
+                yb[k] = (FULL || (k < nb && base + 1 + k < E)) ? y[(size_t)(base + 1 + k) * C] : real(0);
         }
 #pragma unroll
         for (int k = 0; k < B; ++k) {
             const real m = shfl_idx_(fm, k), lm = shfl_idx_(flm, k), ih = shfl_idx_(fih, k);
-            if (k < nb) {
+            if (FULL || k < nb) {
                 const int i = base + k;
                 const real ynext = yb[k];
                 real slope = real(0), r = real(0);
-                if (i < E - 1) slope = mul_(sub_(ynext, yi), ih);
+                if (FULL || i < E - 1) slope = mul_(sub_(ynext, yi), ih);
                 // identity rows (record ends) have lm = 0 and m = 1; a not-a-knot
                 // row 1 also has lm = 0, so NAK tells them apart by m
                 if (NAK ? !is_one(m) : !is_zero(lm)) {
@@ -648,7 +652,7 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 }
                 const real dcur = fmad_(-lm, dprev, mul_(m, r));
                 // rows before i0 only warm the recurrence up
-                if (i >= i0) {
+                if (FULL || i >= i0) {
                     if (cok) o[(size_t)i * C] = dcur;
                     ymax = fmaxf(ymax, magf(yi));
                 }
@@ -657,6 +661,10 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 dprev = dcur;
             }
         }
+    };
+    for (int base = is; base < i1; base += B) {
+        if (base >= i0 && base + B <= i1 && base + B < E) batch(std::true_type{}, base);
+        else batch(std::false_type{}, base);
     }
     if (bnd && cok) {
         if (i1 < E) ymax = fmaxf(ymax, magf(yi));  // right end of the last piece
@@ -691,8 +699,11 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     const int ie = (H < 0) ? E : min(E, i1 + H);
     real snext = real(0), snext2 = real(0);
     float spart = 0.0f;
-    for (int top = ie - 1; top >= i0; top -= B) {
-        const int nb = min(B, top - i0 + 1);
+    // one batch of B rows from top down; FULL (a compile-time flag): all B
+    // rows are owned (>= i0, < i1) and have a right neighbour
+    auto batch = [&](auto full, int top) {
+        constexpr bool FULL = decltype(full)::value;
+        const int nb = FULL ? B : min(B, top - i0 + 1);
         real fcp = real(0), fih = real(0);
         if (lane < nb) {
             const Fac<real> fr = f[top - lane];
@@ -701,20 +712,20 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
         }
         real db[B];
 #pragma unroll
-        for (int k = 0; k < B; ++k) db[k] = (k < nb) ? d[(size_t)(top - k) * C] : real(0);
+        for (int k = 0; k < B; ++k) db[k] = (FULL || k < nb) ? d[(size_t)(top - k) * C] : real(0);
 #pragma unroll
         for (int k = 0; k < B; ++k) {
             const real cp = shfl_idx_(fcp, k), ihr = shfl_idx_(fih, k);
-            if (k < nb) {
+            if (FULL || k < nb) {
                 const int i = top - k;
                 real sol = fmad_(-cp, snext, db[k]);
                 if constexpr (NAK) {
                     if (nak && i == 0)
                         sol = add_(snext, div_(mul_(sub_(snext, snext2), real(kn[1] - kn[0])), real(kn[2] - kn[1])));
                 }
-                if (i < i1) {
+                if (FULL || i < i1) {
                     if (cok && !(NAK && nak && i == E - 1)) o[(size_t)i * C] = sol;
-                    if (bnd && i < E - 1) {
+                    if (bnd && (FULL || i < E - 1)) {
                         // h^2 = 1 / ih^2 (9 / ih^2 when ih holds 3/h); the approximate
                         // division's error is inside the 1.01 margin applied at the end
                         const float ih = magf(ihr);
@@ -734,6 +745,10 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
                 snext = sol;
             }
         }
+    };
+    for (int top = ie - 1; top >= i0; top -= B) {
+        if (!NAK && top - B + 1 >= i0 && top < i1 && top < E - 1) batch(std::true_type{}, top);
+        else batch(std::false_type{}, top);
     }
     if (bnd && cok) atomicMax(&bnd[C + it.c], __float_as_uint(spart * 1.01f));
 }

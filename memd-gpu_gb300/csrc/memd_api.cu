@@ -318,9 +318,14 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
         lc.begin();
-        k_factor<R><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
-                                                                 (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
-                                                                 p->cum ? p->cumcfg : nullptr, p->ep);
+        if (g.nak)
+            k_factor<R, true><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
+                                                                       (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
+                                                                       p->cum ? p->cumcfg : nullptr, p->ep);
+        else
+            k_factor<R, false><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
+                                                                        (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
+                                                                        p->cum ? p->cumcfg : nullptr, p->ep);
         lc.end(MEMD_STAGE_FACTOR);
         const long nseg = (p->H < 0) ? 1 : (g.cap + p->Ss - 1) / p->Ss;
         const long ns = 2L * kc * nseg * p->ngroups * 32;

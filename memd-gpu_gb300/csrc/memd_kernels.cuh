@@ -369,7 +369,7 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
 // the window reaches row 0, whose pivot is 1 with cp = 0; otherwise the
 // start error decays by at least 1/3 per row).  rtab[h] = 1/h.
 // ---------------------------------------------------------------------------
-template <typename real>
+template <typename real, bool NAK>
 __global__ void __launch_bounds__(128)
 k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real* __restrict__ rtab,
          Fac<real>* __restrict__ fac, Geom g, int k0, int Kc, int Sf, int Hf, int* __restrict__ cumcfg,
@@ -430,50 +430,63 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
     int xl = js > 0 ? x[js - 1] : 0;
     int xi = x[js];
     constexpr int FB = 8;  // knot positions loaded per batch (independent loads)
-    for (int base = js; base < i1; base += FB) {
+    // FULL (compile-time): all FB rows are owned (>= i0, < i1) and have a right
+    // neighbour, so no row needs a guard
+    auto batch = [&](auto full, int base) {
+        constexpr bool FULL = decltype(full)::value;
         int xs[FB];
 #pragma unroll
         for (int k = 0; k < FB; ++k) {
             const int i = base + k;
-            xs[k] = (i < i1 && i < E - 1) ? x[i + 1] : 0;
+            xs[k] = (FULL || (i < i1 && i < E - 1)) ? x[i + 1] : 0;
         }
 #pragma unroll
         for (int k = 0; k < FB; ++k) {
             const int i = base + k;
-            if (i < i1) {
-                const int xr = (i < E - 1) ? xs[k] : xi;
+            if (FULL || i < i1) {
+                const int xr = (FULL || i < E - 1) ? xs[k] : xi;
                 real l, d, u;
-                int wn = 0, wd = 0;  // right-hand-side weight wn / wd of a not-a-knot row
+                bool wrow = false;  // a not-a-knot row: right-hand side weighted by wn / wd
+                int wn = 0, wd = 1;
                 if (record_end_knot(ep, xi, i, E)) {  // natural end conditions: s = 0
                     l = real(0); d = real(1); u = real(0);
                 } else {
                     const int hl = xi - xl, hr = xr - xi;
                     l = real(hl); u = real(hr); d = real(2 * (hl + hr));
-                    if (g.nak && E >= 4 && i == 1) {
-                        // s_0 eliminated by the not-a-knot condition d_0 = d_1
-                        l = real(0); d = real(hl + 2 * hr); u = real(hr - hl);
-                        wn = hr; wd = hl + hr;
-                    } else if (g.nak && E >= 4 && i == E - 2) {
-                        // s_{E-1} eliminated by d_{E-3} = d_{E-2}
-                        l = real(hl - hr); d = real(2 * hl + hr); u = real(0);
-                        wn = hl; wd = hl + hr;
+                    if constexpr (NAK) {
+                        if (E >= 4 && i == 1) {
+                            // s_0 eliminated by the not-a-knot condition d_0 = d_1
+                            l = real(0); d = real(hl + 2 * hr); u = real(hr - hl);
+                            wrow = true; wn = hr; wd = hl + hr;
+                        } else if (E >= 4 && i == E - 2) {
+                            // s_{E-1} eliminated by d_{E-3} = d_{E-2}
+                            l = real(hl - hr); d = real(2 * hl + hr); u = real(0);
+                            wrow = true; wn = hl; wd = hl + hr;
+                        }
                     }
                 }
                 const real gp = fmad_(-l, cp, d);
                 const real m = recip_(gp);
                 cp = mul_(u, m);
-                if (i >= i0) {
+                if (FULL || i >= i0) {
                     Fac<real> o;
-                    o.m = wd ? mul_(m, div_(real(wn), real(wd))) : m;
+                    o.m = m;
+                    if constexpr (NAK) {
+                        if (wrow) o.m = mul_(m, div_(real(wn), real(wd)));
+                    }
                     o.lm = mul_(l, m);
                     o.cp = cp;
-                    o.ih = (i < E - 1) ? fac_ih(rtab[xr - xi]) : real(0);
+                    o.ih = (FULL || i < E - 1) ? fac_ih(rtab[xr - xi]) : real(0);
                     f[i] = o;
                 }
                 xl = xi;
                 xi = xr;
             }
         }
+    };
+    for (int base = js; base < i1; base += FB) {
+        if (base >= i0 && base + FB <= i1 && base + FB < E) batch(std::true_type{}, base);
+        else batch(std::false_type{}, base);
     }
 }
 

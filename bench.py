@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-epochs measurement")
     ap.add_argument("--no-long", action="store_true", help="skip the long-record measurement")
+    ap.add_argument("--no-wide", action="store_true", help="skip the 128-channel record measurement")
     return ap.parse_args()
 
 
@@ -359,11 +360,18 @@ def run_ours(args):
         bres = batched_epochs(rank)
         if rank == 0:
             line["batched_epochs"] = bres
+    if not args.no_wide:
+        for p in plans.values():
+            p.close()
+        plans = {}
+        wres = single_record(rank, WIDE)
+        if rank == 0:
+            line["wide_record"] = wres
     if not args.no_long:
         for p in plans.values():
             p.close()
         plans = {}
-        lres = long_record(rank)
+        lres = single_record(rank, LONG)
         if rank == 0:
             line["long_record"] = lres
     if ws > 1:
@@ -442,20 +450,24 @@ def batched_epochs(rank):
 # long record: 64 channels x 262,144 samples (fs 512 Hz), 256 directions,
 # 12 IMF slots x 10 sifts (fixed mode); beyond the reference's int32 indexing
 LONG = dict(workload="long64_262144_k256_fixed", C=64, L=262144, K=256, num_imfs=12, max_iter=10, fs=512.0,
-            warmup=1, steps=1)
+            warmup=1, steps=1, seed=500)
+# wide record: 128 channels x 10,000 samples (fs 256 Hz), 256 directions,
+# 9 IMF slots x 10 sifts (fixed mode)
+WIDE = dict(workload="wide128_10000_k256_fixed", C=128, L=10000, K=256, num_imfs=9, max_iter=10, fs=256.0,
+            warmup=1, steps=2, seed=700)
 
 
-def long_record(rank):
-    """Mixed-form channel-samples/s on the long record, the per-IMF gate against
-    the FP64 path, and the mean HBM rate of the decomposition's algorithmic
-    traffic (knot arrays and signal, from a traced run's knot counts)."""
+def single_record(rank, Lr):
+    """Mixed-form channel-samples/s on one record (the long or the wide one),
+    the per-IMF gate against the FP64 path, and the mean HBM rate of the
+    decomposition's algorithmic traffic (knot arrays and signal, from a traced
+    run's knot counts)."""
     import torch
 
     import memd_gb300 as mg
 
-    Lr = LONG
     C, L, K, NI, IT = Lr["C"], Lr["L"], Lr["K"], Lr["num_imfs"], Lr["max_iter"]
-    y = mg.synth_eeg(C, L, Lr["fs"], seed=500 + rank).astype(np.float32)
+    y = mg.synth_eeg(C, L, Lr["fs"], seed=Lr["seed"] + rank).astype(np.float32)
     d32 = mg.directions(C, K, dtype="f32")
     stream = torch.cuda.current_stream()
     out = {"workload": Lr["workload"], "C": C, "L": L, "K": K, "num_imfs": NI, "max_iter": IT}

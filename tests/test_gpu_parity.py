@@ -253,7 +253,7 @@ def test_mixed_stop_mode_runs():
 
 
 @pytest.mark.parametrize("C,L,K,chunk", [(8, 2000, 64, 0), (5, 3000, 16, 0), (40, 4000, 24, 0),
-                                         (32, 8192, 64, 0), (12, 5000, 40, 16)])
+                                         (32, 8192, 64, 0), (12, 5000, 40, 16), (128, 10000, 256, 0)])
 def test_mixed_impulse_mean_matches_fp64_sets(C, L, K, chunk):
     """Mixed form, fixed mode: the impulse-accumulation mean (default) and the
     direct evaluation of every envelope give the FP64 path's extrema sets at

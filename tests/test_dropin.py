@@ -133,3 +133,10 @@ def test_sweep_prints_the_reference_table():
     rows = [tuple(x.strip() for x in l.split(",")) for l in lines[1:]]
     assert [(int(a), int(b), int(c)) for a, b, c, _ in rows] == [(C, L, 8) for C in (4, 8) for L in (500, 1000, 1500)]
     assert all(float(t) > 0 for *_, t in rows)
+
+
+def test_profile_case_usage():
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(os.path.dirname(BIN), "examples", "profile_case.py"), "--help"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0 and "eeg32" in r.stdout and "batched" in r.stdout

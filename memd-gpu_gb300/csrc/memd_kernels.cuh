@@ -39,6 +39,9 @@
 namespace memd {
 
 constexpr unsigned kFull = 0xffffffffu;
+// longest anchor span of the impulse-accumulation mean: 4 words = 128
+// samples (its accumulators then fit four CTAs per SM, at 64 registers)
+constexpr int kCumMaxWords = 4;
 constexpr int kTrace = 1;
 
 // ---------------------------------------------------------------------------
@@ -376,7 +379,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
          Epochs ep)
 {
     // cumcfg != nullptr (impulse-accumulation mean): block 0 picks the mean
-    // kernel's anchor span, 32 m samples (m the largest power of two <= 8 with
+    // kernel's anchor span, 32 m samples (m the largest power of two <= 4 with
     // 32 m <= 2 h, h the chunk's mean knot spacing, so that rounding carried
     // across a span grows by at most ~(32m/h)^2 = 4 over a direct evaluation;
     // at the densest knots m = 1), and splits each span's (direction,
@@ -397,7 +400,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             int m = 1;
             if (et > 0) {
                 const double h = (double)g.L * (2.0 * q) / (double)et;
-                while (m < 8 && 32.0 * (2 * m) <= 2.0 * h) m *= 2;
+                while (m < kCumMaxWords && 32.0 * (2 * m) <= 2.0 * h) m *= 2;
             }
             // parts per span: the fewest (a power of two <= m) that still give
             // the launch ~2048 working CTAs; a long record or a batch has
@@ -1227,7 +1230,7 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
 // (n - x)_+^3 is 1, 4, 1 at n = x-3, x-2, x-1 and zero elsewhere, so the sum
 // over all envelopes M(n) = sum_e S_e(n) obeys
 //     Delta^4 M(n) = I(n) = sum over interior knots of dd_j * {1,4,1}.
-// Per span of 32 m samples (m = 1 .. 8 words, longer where the knots are
+// Per span of 32 m samples (m = 1 .. 4 words, longer where the knots are
 // sparse) the kernel anchors M at the middle sample n_a (value and the first
 // three forward differences of the pieces active there, plus the impulses that
 // knots at n_a+1, n_a+2 place before n_a), then rebuilds M(n) by running the
@@ -1322,8 +1325,7 @@ __device__ __forceinline__ dd fix2dd(unsigned long long v, int sh)
     return neg ? dd(-hi, -lo) : dd(hi, lo);
 }
 
-constexpr int kCumMaxWords = 8;  // longest anchor span: 8 words = 256 samples
-constexpr int kCumMaxParts = 8;  // most CTAs sharing one span
+constexpr int kCumMaxParts = 4;  // most CTAs sharing one span
 
 // Global accumulators of the spans split over several CTAs (zero between
 // launches: the CTA that finishes a span clears them).
@@ -1334,7 +1336,7 @@ struct CumShared {
 };
 
 template <int G>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 4)
 k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restrict__ acc_buf,
            const uint32_t* __restrict__ bits,
            const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
@@ -1358,7 +1360,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const int C = g.C;
     const int mw = min(max(cumcfg[0], 1), kCumMaxWords), P = min(max(cumcfg[1], 1), kCumMaxParts);
     // CTA b works on part b % P of span b / P (launched: W rounded up to a
-    // multiple of 8 CTAs, so that every part of every span exists; P | m | 8)
+    // multiple of 4 CTAs, so that every part of every span exists; P | m | 4)
     const int si = blockIdx.x / P, prt = blockIdx.x % P;
     const int w = si * mw;
     if (bnd_clear && blockIdx.x == 0 && blockIdx.y == 0)

@@ -502,8 +502,8 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
 //   k_solve_bwd: backward sweep from i1+H-1 down to i0, reading d of the
 //                segment and of the next segment's first H rows from dbuf,
 //                writing the solution of rows [i0, i1) to sv.
-// Rows go in batches of 16: every lane loads its 16 values at once, lanes
-// 0..15 load the batch's factor rows, which the sweep takes by shuffle, so a
+// Rows go in batches of 8: every lane loads its 8 values at once, lanes
+// 0..7 load the batch's factor rows, which the sweep takes by shuffle, so a
 // batch costs one memory round trip instead of one per row.
 // Both recurrences contract (multipliers <= 2/3 and <= 1/2 per row), so a
 // window's truncated start perturbs the segment by at most that factor to the
@@ -519,7 +519,7 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
 // bits; their sum bounds |S(n)| (the linear interpolant plus h^2/8 max|S''|).
 // ---------------------------------------------------------------------------
 constexpr int kSolveThreads = 128;
-constexpr int kSolveBatch = 16;
+constexpr int kSolveBatch = 8;
 
 struct SolveItem {
     int env, kk, seg, c, i0, i1, E;

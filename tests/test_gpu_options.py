@@ -105,3 +105,19 @@ def test_default_options_unchanged():
     a, _, _ = run_gpu(y, d, 3, 3)
     b, _, _ = run_gpu(y, d, 3, 3, spline_end=mg.SPLINE_NATURAL, boundary=mg.BOUNDARY_REFERENCE)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("boundary", [mg.BOUNDARY_REFERENCE, mg.BOUNDARY_MIRROR])
+def test_f64_multi_chunk_compaction_matches_oracle(boundary):
+    # 140,000 samples = 4,375 bitmask words: the knot lists are written by two
+    # compaction CTAs per (direction, envelope), the second finishing the slot
+    y = mg.synth_eeg(2, 140000, 256.0, 66)
+    d = oracle.directions(2, 6)
+    nimf, it = 3, 2
+    imfs, st, tr = run_gpu(y, d, nimf, it, trace=True, boundary=boundary)
+    oimfs, info = oracle.memd(y, d, nimf, it, trace=True, boundary=boundary)
+    assert np.array_equal(tr["count"], info["trace"]["count"])
+    assert np.array_equal(tr["hash"], info["trace"]["hash"])
+    for i in range(nimf):
+        assert rel_l2(imfs[i], oimfs[i]) < 1e-10, i
+    assert st.flags == 0

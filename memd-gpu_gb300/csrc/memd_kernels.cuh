@@ -1244,12 +1244,15 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
 // are exact and independent of their order; each lane's anchor coefficients
 // are summed in double-float in a fixed order before quantisation.  The
 // double-float inputs carry ~48 bits, and the recurrence extrapolates each
-// anchor over at most 16 m samples, 16 m <= 4.5 mean knot spacings, which keeps
-// the mean within ~1e-13 of its value relative to the signal (the direct
-// evaluation: ~1e-15).
+// anchor over at most 16 m samples (one mean knot spacing where the knots are
+// sparse enough for m > 1; 16 samples at the densest), which keeps the mean
+// within ~1e-13 of its value relative to the signal (the direct evaluation:
+// ~1e-15).  The conversions round to nearest: truncation's one-sided error
+// accumulates over the sifts.
 //
 // CTA: one span (or one of the P parts of a span's directions) x G channels,
-// 8 warps; lane = (subgroup, channel), the (direction,
+// 8 warps, four CTAs per SM (64 registers; the accumulators of a span of at
+// most 128 samples take 33.5 KB); lane = (subgroup, channel), the (direction,
 // envelope) pairs are dealt round-robin to the 8 * 32/G subgroups, which add
 // each knot's jump into a per-row array in shared memory (one 64-bit integer
 // atomic per knot).  The recurrence runs as four block-wide exact prefix sums
@@ -1367,7 +1370,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
         for (int i = threadIdx.x; i < 2 * C; i += blockDim.x) bnd_clear[i] = 0u;
     if (w >= g.W) return;  // uniform over the CTA
     // the record (epoch) of the span; spans never straddle two (epochs start at
-    // multiples of kEpochAlign = 512 samples, spans are at most 256 long)
+    // multiples of kEpochAlign = 512 samples, spans are at most 128 long)
     const int rec = ep.n > 0 ? ep.wep[w] : 0;
     const int rend = ep.n > 0 ? ep.off[rec] + ep.len[rec] : g.L;  // one past the record's last sample
     const int p0 = w * 32;

@@ -66,15 +66,15 @@ k_project_extrema(const XT* __restrict__ X, const real* __restrict__ dir,
     real* ps = ds + kProjTK * C;                              // TK x (TN + 2)
     const int n0 = blockIdx.x * kProjTN;
     const int kt0 = blockIdx.y * kProjTK;
-    for (int idx = threadIdx.x; idx < (kProjTN + 2) * C; idx += blockDim.x) {
-        const int r = idx / C, c = idx - r * C;
+    // tile loads: rows by warp, channels by lane (no division by C)
+    for (int r = threadIdx.x >> 5; r < kProjTN + 2; r += blockDim.x >> 5) {
         const int n = n0 - 1 + r;
-        xs[r * ldx + c] = (n >= 0 && n < g.L) ? xval<real>(X[(size_t)n * C + c]) : real(0);
+        for (int c = threadIdx.x & 31; c < C; c += 32)
+            xs[r * ldx + c] = (n >= 0 && n < g.L) ? xval<real>(X[(size_t)n * C + c]) : real(0);
     }
-    for (int idx = threadIdx.x; idx < kProjTK * C; idx += blockDim.x) {
-        const int kk = idx / C, c = idx - kk * C;
+    for (int kk = threadIdx.x >> 5; kk < kProjTK; kk += blockDim.x >> 5) {
         const int k = kt0 + kk;
-        ds[idx] = (k < Kc) ? dir[(size_t)(k0 + k) * C + c] : real(0);
+        for (int c = threadIdx.x & 31; c < C; c += 32) ds[kk * C + c] = (k < Kc) ? dir[(size_t)(k0 + k) * C + c] : real(0);
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1698,16 +1698,18 @@ k_project_mx(const float2* __restrict__ X, const float* __restrict__ dh_all, con
     float* dls = bnd + kProjTK;                            // TK x C (low words)
     const int n0 = blockIdx.x * kProjTN;
     const int kt0 = blockIdx.y * kProjTK;
-    for (int idx = threadIdx.x; idx < (kProjTN + 2) * C; idx += blockDim.x) {
-        const int r = idx / C, c = idx - r * C;
+    // tile loads: rows by warp, channels by lane (no division by C)
+    for (int r = threadIdx.x >> 5; r < kProjTN + 2; r += blockDim.x >> 5) {
         const int n = n0 - 1 + r;
-        xs[r * ldx + c] = (n >= 0 && n < g.L) ? X[(size_t)n * C + c].x : 0.f;
+        for (int c = threadIdx.x & 31; c < C; c += 32)
+            xs[r * ldx + c] = (n >= 0 && n < g.L) ? X[(size_t)n * C + c].x : 0.f;
     }
-    for (int idx = threadIdx.x; idx < kProjTK * C; idx += blockDim.x) {
-        const int kk = idx / C, c = idx - kk * C;
+    for (int kk = threadIdx.x >> 5; kk < kProjTK; kk += blockDim.x >> 5) {
         const int k = kt0 + kk;
-        ds[idx] = (k < Kc) ? dh_all[(size_t)(k0 + k) * C + c] : 0.f;
-        dls[idx] = (k < Kc) ? dl_all[(size_t)(k0 + k) * C + c] : 0.f;
+        for (int c = threadIdx.x & 31; c < C; c += 32) {
+            ds[kk * C + c] = (k < Kc) ? dh_all[(size_t)(k0 + k) * C + c] : 0.f;
+            dls[kk * C + c] = (k < Kc) ? dl_all[(size_t)(k0 + k) * C + c] : 0.f;
+        }
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

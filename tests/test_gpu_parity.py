@@ -297,3 +297,24 @@ def test_long_record_mixed_runs_and_matches_fp64():
     for i in range(3):
         assert rel_l2(b[i], a[i]) < 1e-6, i
     assert np.abs(b.astype(np.float64).sum(axis=0) - y).max() < 1e-4 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("precision", [mg.PREC_F64, mg.PREC_MIXED])
+def test_two_tone_separation_on_gpu(precision):
+    """Known answer: a 60 Hz and a 5 Hz tone in two channels come out as the
+    first IMF and the rest, away from the record's ends."""
+    L, fs = 2000, 1000.0
+    n = np.arange(L) / fs
+    hi = np.stack([np.sin(2 * np.pi * 60 * n), 0.7 * np.sin(2 * np.pi * 60 * n + 1.0)])
+    lo = np.stack([np.sin(2 * np.pi * 5 * n + 0.3), 1.3 * np.sin(2 * np.pi * 5 * n + 2.0)])
+    y = hi + lo
+    d = oracle.directions(2, 16)
+    if precision == mg.PREC_MIXED:
+        y, d = y.astype(np.float32), d.astype(np.float32)
+    imfs, st, _ = run_gpu(y, d, 3, 10, precision=precision)
+    imfs = imfs.astype(np.float64)
+    core = slice(200, L - 200)
+    assert np.linalg.norm(imfs[0][:, core] - hi[:, core]) / np.linalg.norm(hi[:, core]) < 0.03
+    rest = imfs[1] + imfs[2]
+    assert np.linalg.norm(rest[:, core] - lo[:, core]) / np.linalg.norm(lo[:, core]) < 0.03
+    assert st.flags == 0

@@ -84,3 +84,31 @@ def test_stop_mode_terminates_and_telescopes():
 def test_window_cover_formula(L):
     # 240 interior samples per block of 242, ceil(L / 242) blocks
     assert oracle.window_cover(L) == 240 * ((L + 241) // 242)
+
+
+def _tones(freqs_amps, L=2000, fs=1000.0):
+    n = np.arange(L) / fs
+    return np.stack([sum(a * np.sin(2 * np.pi * f * n + ph) for f, a, ph in ch) for ch in freqs_amps])
+
+
+def _rel_core(a, b, edge=200):
+    core = slice(edge, a.shape[1] - edge)
+    return np.linalg.norm(a[:, core] - b[:, core]) / np.linalg.norm(b[:, core])
+
+
+def test_two_tone_separation():
+    """Two well-separated tones (60 and 5 Hz, two channels with their own
+    amplitudes and phases): the first IMF is the fast tone and the remaining
+    slots add up to the slow one, away from the record's ends."""
+    hi = _tones([[(60, 1.0, 0.0)], [(60, 0.7, 1.0)]])
+    lo = _tones([[(5, 1.0, 0.3)], [(5, 1.3, 2.0)]])
+    imfs, _ = oracle.memd(hi + lo, oracle.directions(2, 16), 3, 10)
+    assert _rel_core(imfs[0], hi) < 0.03
+    assert _rel_core(imfs[1] + imfs[2], lo) < 0.03
+
+
+def test_single_tone_is_one_imf():
+    y = _tones([[(20, 1.0, 0.0)], [(20, 0.5, 0.5)]])
+    imfs, _ = oracle.memd(y, oracle.directions(2, 16), 2, 10)
+    assert _rel_core(imfs[0], y) < 0.01
+    assert np.abs(imfs[1][:, 200:-200]).max() < 0.02

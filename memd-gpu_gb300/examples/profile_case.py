@@ -29,6 +29,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--runs", type=int, default=1)
     a = ap.parse_args()
+    if a.runs < 1:
+        ap.error("--runs must be at least 1")
     prec = {"mixed": mg.PREC_MIXED, "f64": mg.PREC_F64, "f32": mg.PREC_F32}[a.precision]
     tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
     if a.case == "eeg32":

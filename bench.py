@@ -67,6 +67,29 @@ def dist_env():
     return ws, rank, local
 
 
+def _reduce_over_ranks(x: float, device, op_name: str) -> float:
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=getattr(dist.ReduceOp, op_name))
+    return float(t.item())
+
+
+def max_over_ranks(x: float, device="cuda") -> float:
+    """Largest x over the ranks of the process group (x itself on one rank):
+    the timed region of a replicated run ends when its slowest rank does."""
+    return _reduce_over_ranks(x, device, "MAX")
+
+
+def sum_over_ranks(x: float, device="cuda") -> float:
+    """Sum of x over the ranks (x itself on one rank): the units of work that
+    all replicas processed."""
+    return _reduce_over_ranks(x, device, "SUM")
+
+
 # ----------------------------------------------------------------------------
 # clocks sampling (nvidia-smi during the timed region)
 # ----------------------------------------------------------------------------
@@ -212,11 +235,9 @@ def run_ours(args):
         torch.cuda.synchronize()
         ck = clocks.stop() if clocks else None
         ms = [a.elapsed_time(b) for a, b in ev]
-        tot = torch.tensor([sum(ms)], dtype=torch.float64, device="cuda")
-        if ws > 1:
-            dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+        tot = max_over_ranks(sum(ms))
         st = plan.run(dy, d, out, stats=True)
-        results[name] = {"ms_per_step": float(tot.item()) / args.steps, "wall_s": wall, "clocks": ck,
+        results[name] = {"ms_per_step": tot / args.steps, "wall_s": wall, "clocks": ck,
                          "launches_per_step": int(st.launches), "flags": int(st.flags), "refined": int(st.refined),
                          "workspace_gb": plan.workspace_bytes / 1e9}
         outs[name] = (out, d, dy)
@@ -254,10 +275,7 @@ def run_ours(args):
         hout.copy_(dout, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = torch.tensor([e0.elapsed_time(e1) / args.steps], dtype=torch.float64, device="cuda")
-    if ws > 1:
-        dist.all_reduce(e2e_ms, op=dist.ReduceOp.MAX)
-    e2e_ms = float(e2e_ms.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     elem = 8 if head == "fp64" else 4
 
     # per-stage timing (eager, every kernel bracketed by CUDA events) and knot
@@ -428,9 +446,10 @@ def batched_epochs(rank):
             plan.run_batched(y, lengths, offs, d, o, stream=stream, stats=False)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / B["steps"]
+        ms = max_over_ranks(e0.elapsed_time(e1) / B["steps"])
         st = plan.run_batched(y, lengths, offs, d, o)
-        out[name] = {"ms_per_step": ms, "channel_samples_per_s": C * float(lengths.sum()) / (ms / 1e3),
+        units = sum_over_ranks(C * float(lengths.sum()))  # every replica decomposes its own epoch set
+        out[name] = {"ms_per_step": ms, "channel_samples_per_s": units / (ms / 1e3),
                      "workspace_gb": plan.workspace_bytes / 1e9, "flags": int(st.flags)}
         outs[name] = o.cpu().numpy().astype(np.float64)
         plan.close()
@@ -486,9 +505,9 @@ def single_record(rank, Lr):
             plan.run(dy, d, o, stream=stream, stats=False)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / Lr["steps"]
+        ms = max_over_ranks(e0.elapsed_time(e1) / Lr["steps"])
         st = plan.run(dy, d, o)
-        entry = {"ms_per_step": ms, "channel_samples_per_s": C * L / (ms / 1e3),
+        entry = {"ms_per_step": ms, "channel_samples_per_s": sum_over_ranks(C * L) / (ms / 1e3),
                  "workspace_gb": plan.workspace_bytes / 1e9, "flags": int(st.flags)}
         if name == "mixed":
             plan.set_trace(True)

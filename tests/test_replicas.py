@@ -39,7 +39,7 @@ def _rank_main(rank, world, port, results):
 
 def test_two_replicas_take_the_slowest_rank_and_all_units():
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         results = mgr.dict()
         mp.spawn(_rank_main, args=(2, port, results), nprocs=2, join=True)
         got = dict(results)

@@ -234,10 +234,12 @@ memd_status memd_directions_f32(int64_t channels, int64_t directions, const int3
  * application that hands out all device memory from one arena it owns.  It
  * allocates nothing: the prime table lives in a static device array of 4096
  * entries, so channels > 4096 is rejected (MEMD_ERR_INVALID).  The array is
- * shared by all calls: calls whose copies and kernels overlap on the GPU (for
- * example on two streams) race and must be ordered by the caller.  The first
- * call on each device looks up the array's device address; make that first
- * call before any stream capture that includes this entry point.
+ * shared by all calls and keeps the last call's table: calls whose copies and
+ * kernels overlap on the GPU (for example on two streams) race and must be
+ * ordered by the caller.  Each call looks up the array's address in the
+ * current context (cudaGetSymbolAddress, which allocates nothing), so a device
+ * reset between calls is harmless.  The table is copied from host stack
+ * memory with cudaMemcpyAsync on the given stream.
  * No counterpart in the reference (which always allocates its tables). */
 memd_status memd_directions_noalloc_f64(int64_t channels, int64_t directions, const int32_t* primes,
                                         double* d_dir, void* stream);

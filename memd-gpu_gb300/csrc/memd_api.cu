@@ -633,6 +633,11 @@ static memd_status batched_inputs(memd_plan* p, int n, const int64_t* lengths, c
     cudaError_t e;
     std::vector<int64_t> lens(lengths, lengths + n);
     if (lens != p->ep_lens || !p->exec) {
+        // A run still in flight on s may be reading the epoch table (its graph
+        // and k_batched_out): let it finish before the table and the graph
+        // change.  Only a change of the length set takes this path.
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return set_cuda_error("run_batched: synchronize before a new layout", e);
         // layout: off[e] = sum of the earlier lengths rounded up to kEpochAlign
         const int me = (int)p->cfg.max_epochs;
         std::vector<int> off(n), cov(n), w0(n + 1);
@@ -657,7 +662,11 @@ static memd_status batched_inputs(memd_plan* p, int n, const int64_t* lengths, c
         int* wep = h + 4 * me + 1;
         for (int i = 0; i < n; ++i)
             for (int w = w0[i]; w < w0[i + 1]; ++w) wep[w] = i;
-        e = cudaMemcpy(p->ep_dev, h, sizeof(int) * p->ep_host.size(), cudaMemcpyHostToDevice);
+        // stream-ordered copy on the caller's stream; the host staging vector
+        // is rewritten only on the next layout change, after the synchronise
+        // above
+        e = cudaMemcpyAsync(p->ep_dev, h, sizeof(int) * p->ep_host.size(), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return set_cuda_error("run_batched: epoch table", e);
         p->ep.n = n;
         p->ep.off = p->ep_dev;

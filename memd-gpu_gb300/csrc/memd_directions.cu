@@ -12,7 +12,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
-#include <mutex>
 #include <vector>
 
 #include "memd_device.cuh"
@@ -113,32 +112,24 @@ static memd_status directions_impl(int64_t C, int64_t K, const int32_t* primes, 
 // file-scope device array instead of a per-call allocation.  The array holds
 // kNoAllocMaxChannels entries on every GPU that loads the library, until the
 // process exits.  Host code may not hand the array's name to a kernel (on the
-// host it is only a stand-in for the device symbol), so its device address is
-// looked up once per device with cudaGetSymbolAddress and cached.
+// host it is only a stand-in for the device symbol), so every call looks up
+// its device address with cudaGetSymbolAddress, with the caller's device and
+// context current.  The lookup allocates nothing and costs a few
+// microseconds; an address kept from an earlier call could belong to a
+// context that has since been destroyed (cudaDeviceReset, a MATLAB
+// reset(gpuDevice) while the MEX file stays loaded) or to another context on
+// the same device.
 // ---------------------------------------------------------------------------
 constexpr int kNoAllocMaxChannels = 4096;
 static __device__ __align__(256) int g_noalloc_primes[kNoAllocMaxChannels];
 
-static std::mutex g_noalloc_mu;
-constexpr int kMaxDevices = 256;
-static int* g_noalloc_addr[kMaxDevices] = {};
-
-// Device address of g_noalloc_primes on the current device; the first call on
-// a device resolves it (with that device current) and caches it.
+// Device address of g_noalloc_primes in the current context.
 static memd_status noalloc_table(int** out)
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return set_cuda_error("directions_noalloc: cudaGetDevice", e);
-    if (dev < 0 || dev >= kMaxDevices) return set_error(MEMD_ERR_INVALID, "directions_noalloc: device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_primes);
-        if (e != cudaSuccess || !ptr) return set_cuda_error("directions_noalloc: cudaGetSymbolAddress", e);
-        g_noalloc_addr[dev] = static_cast<int*>(ptr);
-    }
-    *out = g_noalloc_addr[dev];
+    void* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_primes);
+    if (e != cudaSuccess || !ptr) return set_cuda_error("directions_noalloc: cudaGetSymbolAddress", e);
+    *out = static_cast<int*>(ptr);
     return MEMD_OK;
 }
 

@@ -2,13 +2,25 @@
 
 TEST INFRASTRUCTURE ONLY.  Two steps:
 
-generate()  -- run where the reference checkout is present: reads
-               memReducedEpochs_dev.cu from it and writes two patched copies
-               into oracle/_ref/ (git-ignored, never committed):
+generate()  -- run where the reference checkout is present (its directory is
+               the argument, else $MEMD_REFERENCE_DIR, else the checkout this
+               build was set up with): reads memReducedEpochs_dev.cu from it
+               and writes two patched copies into oracle/_ref/ (git-ignored,
+               never committed), plus a copy of the reference's input fixture
+               EEGsample_32CH_30504.bin (data, used as a parity input):
                  * memd_ref_f32.cu: the reference as shipped, with
                    - line 1472 ("configuration for the input signal", a stray
                      text line that stops nvcc) turned into a comment,
-                   - its main() renamed so ref_driver.cu can supply one;
+                   - its main() renamed so ref_driver.cu can supply one,
+                   - two test hooks that change no arithmetic: after each
+                     D2H copy of the knot counts (:1228 maxima, :1285 minima)
+                     REF_TRACE_HOOK records every direction's knot count and
+                     index-set hash (ref_driver.cu, when asked), and the
+                     fixed 4 MiB gtsv2 buffer (:1144) is allocated with
+                     REF_GTSV_BUFFER_BYTES (the larger of 4 MiB and the
+                     library's own size query for the longest possible knot
+                     list), while REF_GTSV_CHECK compares every per-direction
+                     size query (:1237, :1295) with what was allocated;
                  * memd_ref_f64.cu: the same plus the FP64 switch of the
                    library calls the reference hard-wires to FP32
                    (cublasSgemm -> cublasDgemm at :1182,
@@ -30,12 +42,22 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("MEMD_REFERENCE_DIR") or "/root/reference"
+FIXTURE = "EEGsample_32CH_30504.bin"
 SRC_NAME = "memReducedEpochs_dev.cu"
 
+_SIZE_QUERY = ("cusparseSgtsv2_nopivot_bufferSizeExt(handle_sparse, h_num_extrema[k], SignalDim, currentLowerDia, "
+               "currentMiddleDia, currentUpperDia, currentRightDia, h_num_extrema[k], buffer_size);")
+_COUNTS_MAX = "cudaMemcpy(h_num_extrema, d_num_extrema_max, NumDirVector * sizeof(coord_t), cudaMemcpyDeviceToHost);"
+_COUNTS_MIN = "cudaMemcpy(h_num_extrema, d_num_extrema_min, NumDirVector * sizeof(coord_t), cudaMemcpyDeviceToHost);"
 COMMON_PATCHES = [
     ("\n    configuration for the input signal\n", "\n    // configuration for the input signal\n"),
     ("\nint main()\n", "\nint memd_reference_original_main()\n"),
+    ("cudaMalloc(&buffer, 1024 * 1024 * sizeof(real_t));",
+     "cudaMalloc(&buffer, REF_GTSV_BUFFER_BYTES(1024 * 1024 * sizeof(real_t)));"),
+    (_SIZE_QUERY, _SIZE_QUERY + " REF_GTSV_CHECK(*buffer_size);"),
+    (_COUNTS_MAX, _COUNTS_MAX + " REF_TRACE_HOOK(0, h_num_extrema, d_compactIndex, SignalLength, SignalDim, NumDirVector);"),
+    (_COUNTS_MIN, _COUNTS_MIN + " REF_TRACE_HOOK(1, h_num_extrema, d_compactIndex, SignalLength, SignalDim, NumDirVector);"),
 ]
 F64_PATCHES = [
     ("cublasSgemm(", "cublasDgemm("),
@@ -48,6 +70,7 @@ F64_PATCHES = [
     ("\nvoid runBenchmark()\n", "\n#if 0 /* float-only drivers */\nvoid runBenchmark()\n"),
 ]
 EXPECTED_COUNTS = {
+    _SIZE_QUERY: 2,
     "cublasSgemm(": 1,
     "cusparseSgtsv2_nopivot_bufferSizeExt(": 2,
     "cusparseSgtsv2_nopivot(": 2,
@@ -82,7 +105,18 @@ def generate(ref_dir: str = DEFAULT_REF) -> bool:
         if old != body:
             with open(path, "w") as f:
                 f.write(body)
+    fx = os.path.join(ref_dir, FIXTURE)
+    if os.path.exists(fx):
+        dst = fixture_path()
+        if not os.path.exists(dst) or os.path.getsize(dst) != os.path.getsize(fx):
+            shutil.copyfile(fx, dst)
     return True
+
+
+def fixture_path() -> str:
+    """Where generate() leaves the reference's input fixture (32 x 30,504
+    float32, channel-major); absent where the reference was never present."""
+    return os.path.join(OUT, FIXTURE)
 
 
 def binary(prec: str) -> str:

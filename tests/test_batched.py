@@ -124,3 +124,36 @@ def test_batched_profile_equals_graph_run(prec):
     plan.close()
     assert torch.equal(a, b)
     assert pr["solve"]["launches"] == 2 * (nimf - 1) * it and pr["eval"]["ms"] > 0
+
+
+@pytest.mark.gpu
+def test_batched_two_layouts_on_a_side_stream_without_sync():
+    """Two batched calls with different length sets, back to back on a
+    non-blocking stream with no host synchronisation between them: the second
+    call's new epoch table must not reach the first call's kernels, so each
+    result equals the same call made alone."""
+    torch = pytest.importorskip("torch")
+    C, K, nimf, it = 4, 8, 3, 3
+    la, lb = [900, 1300, 200], [1500, 64, 700, 1100]
+    ra, oa = _epochs(C, la, seed=90)
+    rb, ob = _epochs(C, lb, seed=95)
+    d = oracle.directions(C, K)
+    want_a, _ = _run_batched(ra, la, oa, d, nimf, it, mg.PREC_F64)
+    want_b, _ = _run_batched(rb, lb, ob, d, nimf, it, mg.PREC_F64)
+    plan = mg.Plan(C, 1500, K, nimf, it, precision=mg.PREC_F64, max_epochs=4)
+    side = torch.cuda.Stream()
+    ya = torch.as_tensor(np.concatenate([r.ravel() for r in ra]), device="cuda")
+    yb = torch.as_tensor(np.concatenate([r.ravel() for r in rb]), device="cuda")
+    dd = torch.as_tensor(d, device="cuda")
+    outa = torch.full((nimf * ya.numel(),), float("nan"), dtype=torch.float64, device="cuda")
+    outb = torch.full((nimf * yb.numel(),), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        plan.run_batched(ya, la, oa, dd, outa, stream=side, stats=False)
+        plan.run_batched(yb, lb, ob, dd, outb, stream=side, stats=False)
+    side.synchronize()
+    plan.close()
+    ga, gb = outa.cpu().numpy(), outb.cpu().numpy()
+    for got, want, offs, lens in ((ga, want_a, oa, la), (gb, want_b, ob, lb)):
+        for w, off, L in zip(want, offs, lens):
+            assert np.array_equal(got[nimf * off: nimf * off + nimf * C * L].reshape(nimf, C, L), w, equal_nan=True)

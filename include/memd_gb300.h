@@ -120,7 +120,10 @@ typedef struct {
                               splines */
     int32_t boundary;      /* memd_boundary: how the envelopes are closed at the
                               record's ends */
-    int32_t reserved32;
+    int32_t projection;    /* mixed form: 0 = automatic (tensor cores: 3xTF32
+                              tcgen05.mma with TMA-staged tiles), 1 = CUDA
+                              cores (FP32 fma); both certify every extremum
+                              test against the FP64 projection */
     int64_t reserved[2];
 } memd_config;
 
@@ -133,7 +136,9 @@ typedef struct {
     int32_t refined;       /* mixed precision: extremum tests re-decided in
                               double-float because the FP32 margin was within
                               the projection's error bound */
-    int32_t reserved;
+    int32_t rechecked;     /* mixed precision, tensor-core projection: tests
+                              redone with FP32 dot products because the
+                              tensor-core margin was within its bound */
 } memd_stats;
 
 /* Per-stage device time of one eagerly launched decomposition (every kernel
@@ -155,6 +160,9 @@ typedef struct {
 #define MEMD_FLAG_NO_QUALIFIED_DIRECTION 1  /* a sift had no direction with >3 maxima
                                                and >3 minima: the reference's 0/0 NaN */
 #define MEMD_FLAG_KNOT_OVERFLOW 2           /* internal knot capacity exceeded */
+#define MEMD_FLAG_DEVICE_TIMEOUT 4          /* a bounded device-side wait ran out (a kernel
+                                               gave up on a copy or product it issued);
+                                               the run's results are not valid */
 
 /* One entry per (IMF, sift, direction, envelope) when a trace buffer is
  * given: the extrema index set of that projected direction. */
@@ -248,6 +256,13 @@ memd_status memd_directions_noalloc_f64(int64_t channels, int64_t directions, co
  * GPU for MEMD_PREC_F64 or MEMD_PREC_F32 arithmetic; the denominator of the
  * CUDA-core roofline figures.  No reference counterpart. */
 memd_status memd_diag_fma_rate(int32_t precision, double* flops_per_s);
+
+/* Diagnostic of the device-side failure detection: one CTA waits on an
+ * mbarrier that nothing completes, with the bounded wait the tensor-core
+ * kernels use (limit max_clocks, 1 .. 2^32); *flags receives the run-state
+ * bits the kernel set (MEMD_FLAG_DEVICE_TIMEOUT when the wait gave up).  No
+ * reference counterpart (the reference has no device waits). */
+memd_status memd_diag_wait_timeout(int64_t max_clocks, int32_t* flags);
 
 /* Text of the last error on this thread. */
 const char* memd_last_error(void);

@@ -6,7 +6,10 @@
 // kernel of every sift: reference loop memReducedEpochs_dev.cu:1176-1338) and
 // copies the IMFs out.  Fixed-iteration runs have no data-dependent host
 // control at all, so the graph is captured once per plan and relaunched.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -16,6 +19,7 @@
 
 #include "memd_internal.h"
 #include "memd_kernels.cuh"
+#include "memd_tc.cuh"
 
 namespace memd {
 
@@ -109,6 +113,16 @@ struct memd_plan {
     cudaGraphExec_t exec;
     int64_t graph_launches;
     cudaEvent_t e0, e1;
+    // mixed form, tensor-core projection: tf32 split of the signal and of the
+    // directions ([rows][Cp], zero-padded channels) and their TMA descriptors
+    int tc;          // k_project_tc replaces k_project_mx
+    int Cp;          // channels rounded up to 32
+    int tc_nt;       // directions per tile (MMA N)
+    float* xbig;
+    float* xsmall;
+    float* dbig;
+    float* dsmall;
+    memd::TcMaps maps;
 };
 
 namespace memd {
@@ -133,6 +147,36 @@ static memd_status dev_alloc(memd_plan* p, void** ptr, size_t bytes)
     return MEMD_OK;
 }
 
+// cuTensorMapEncodeTiled from the driver, without linking libcuda
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)f;
+    }
+    return fn;
+}
+
+// TMA descriptor of a row-major float array [rows][cols] (cols a multiple of
+// 32), copied in boxes of 32 columns (128 bytes) x box_rows rows into the
+// 128-byte swizzled shared-memory layout; rows past the end read as zero.
+static bool make_tile_map(CUtensorMap* m, void* base, uint64_t cols, uint64_t rows, uint32_t box_rows)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * sizeof(float)};
+    const cuuint32_t box[2] = {32u, box_rows};
+    const cuuint32_t es[2] = {1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
 // ----- launch accounting / per-stage timing --------------------------------
 // Counts every kernel launch; when a profile is requested, brackets each
 // launch with CUDA events on the launching stream and waits for it.
@@ -141,13 +185,20 @@ struct Launches {
     memd_profile* prof = nullptr;
     cudaEvent_t a = nullptr, b = nullptr;
     cudaStream_t s = nullptr;
-    void begin()
+    // NVTX range per launch named after its stage (visible to profilers that
+    // filter by range, e.g. ncu --nvtx-include "memd/solve/"; a captured graph
+    // carries them only for its capture)
+    void begin(int stage)
     {
+        static const char* const names[MEMD_STAGES] = {"project", "compact", "factor", "solve",
+                                                       "eval",    "other",   "other",  "other"};
+        nvtxRangePushA(names[stage]);
         if (prof) cudaEventRecord(a, s);
     }
     void end(int stage)
     {
         ++count;
+        nvtxRangePop();
         if (!prof) return;
         cudaEventRecord(b, s);
         cudaEventSynchronize(b);
@@ -261,9 +312,12 @@ static cudaError_t set_attrs(memd_plan* p)
         }
     }
     if (e != cudaSuccess) return e;
-    if constexpr (P == MEMD_PREC_MIXED)
+    if constexpr (P == MEMD_PREC_MIXED) {
         e = cudaFuncSetAttribute(k_project_mx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->proj_smem);
-    else
+        if (e == cudaSuccess && p->tc)
+            e = cudaFuncSetAttribute(k_project_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tc_smem_bytes(p->tc_nt));
+    } else
         e = cudaFuncSetAttribute(k_project_extrema<R, XT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)p->proj_smem);
     return e;
@@ -283,18 +337,32 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         const int k0 = ch * p->Kc;
         const int kc = std::min(p->Kc, g.K - k0);
         dim3 pg((unsigned)((g.L + kProjTN - 1) / kProjTN), (unsigned)((kc + kProjTK - 1) / kProjTK));
-        lc.begin();
-        if constexpr (P == MEMD_PREC_MIXED)
-            k_project_mx<<<pg, 256, p->proj_smem, s>>>((const float2*)p->X, (const float*)p->dir,
-                                                       (const float*)p->dir + (size_t)g.K * g.C, p->bits, g, k0, kc, p->st,
-                                                       p->ep);
-        else
+        lc.begin(MEMD_STAGE_PROJECT);
+        if constexpr (P == MEMD_PREC_MIXED) {
+            if (p->tc) {
+                if (ch == 0) {  // the signal's tf32 split, once per sift
+                    const size_t n = (size_t)g.L * p->Cp;
+                    k_split_tf32<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+                        (const float*)p->X, 2, p->xbig, p->xsmall, g.L, g.C, p->Cp);
+                    lc.end(MEMD_STAGE_PROJECT);
+                    lc.begin(MEMD_STAGE_PROJECT);
+                }
+                dim3 tg((unsigned)((g.L + kTcRows - 1) / kTcRows), (unsigned)((kc + kTcMaxN - 1) / kTcMaxN));
+                k_project_tc<<<tg, kTcThreads, tc_smem_bytes(p->tc_nt), s>>>(
+                    p->maps, (const float2*)p->X, (const float*)p->dir, (const float*)p->dir + (size_t)g.K * g.C,
+                    p->bits, g, k0, kc, p->Cp, p->tc_nt, p->st, p->ep);
+            } else {
+                k_project_mx<<<pg, 256, p->proj_smem, s>>>((const float2*)p->X, (const float*)p->dir,
+                                                           (const float*)p->dir + (size_t)g.K * g.C, p->bits, g, k0, kc,
+                                                           p->st, p->ep);
+            }
+        } else
             k_project_extrema<R, XT><<<pg, 256, p->proj_smem, s>>>((const XT*)p->X, (const R*)p->dir, p->bits, g, k0, kc,
                                                                    p->ep);
         lc.end(MEMD_STAGE_PROJECT);
         if (g.mirror) {
             const unsigned mb = (unsigned)((32L * kc + 127) / 128);
-            lc.begin();
+            lc.begin(MEMD_STAGE_PROJECT);
             if constexpr (P == MEMD_PREC_MIXED)
                 k_mirror<float2, float, float2, true><<<mb, 128, 0, s>>>(
                     p->bits, (const float2*)p->X, nullptr, (const float*)p->dir,
@@ -306,18 +374,18 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         }
         const int nch = (g.W + kCompactChunk - 1) / kCompactChunk;
         if (nch > 1) {
-            lc.begin();
+            lc.begin(MEMD_STAGE_COMPACT);
             k_compact_count<<<dim3((unsigned)nch, (unsigned)(2 * kc)), 512, 0, s>>>(p->bits, p->csh.ctot, g, nch);
             lc.end(MEMD_STAGE_COMPACT);
         }
-        lc.begin();
+        lc.begin(MEMD_STAGE_COMPACT);
         k_compact<R, XT><<<dim3((unsigned)nch, (unsigned)(2 * kc)), 512, 0, s>>>(
             p->bits, p->wpref, p->knots, p->cnt, (R*)p->yv, (const XT*)p->X, trace, g, k0, kc, p->st, trace_rows,
             p->cum ? (R*)p->yend : nullptr, p->ep, p->mir, p->csh, nch);
         lc.end(MEMD_STAGE_COMPACT);
         const long nsegf = (g.cap + p->Sf - 1) / p->Sf;
         const long nf = 2L * kc * nsegf;
-        lc.begin();
+        lc.begin(MEMD_STAGE_FACTOR);
         if (g.nak)
             k_factor<R, true><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
                                                                        (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
@@ -331,7 +399,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         const long ns = 2L * kc * nseg * p->ngroups * 32;
         const unsigned nb = (unsigned)((ns + kSolveThreads - 1) / kSolveThreads);
         unsigned* bcur = p->cum ? p->bnd + (size_t)(p->bpass & 1) * 2 * g.C : nullptr;
-        lc.begin();
+        lc.begin(MEMD_STAGE_SOLVE);
         bool xm = false;
 #define MEMD_FWD(XM_, EPB_, NAK_)                                                                               \
     k_solve_fwd<R, XT, XM_, EPB_, NAK_><<<nb, kSolveThreads, 0, s>>>(                                          \
@@ -351,7 +419,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         }
 #undef MEMD_FWD
         lc.end(MEMD_STAGE_SOLVE);
-        lc.begin();
+        lc.begin(MEMD_STAGE_SOLVE);
         if (g.nak)
             k_solve_bwd<R, true><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
                                                              (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
@@ -361,13 +429,13 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
                                                               (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
                                                               p->knots);
         lc.end(MEMD_STAGE_SOLVE);
-        lc.begin();
+        lc.begin(MEMD_STAGE_EVAL);
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
         lc.end(MEMD_STAGE_EVAL);
         ++p->bpass;
         if (p->cum && ch == p->nchunks - 1) std::swap(p->X, p->Xb);  // the next pass reads the updated signal
         if (stop) {
-            lc.begin();
+            lc.begin(MEMD_STAGE_OTHER);
             k_amp<R><<<(unsigned)((g.L + 255) / 256), 256, 0, s>>>((const R*)p->part, (R*)p->amp, p->cnt, g, k0, kc,
                                                                  p->egroups, ch == 0);
             lc.end(MEMD_STAGE_OTHER);
@@ -375,14 +443,14 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
     }
     if (stop) {
         const size_t CL = (size_t)g.C * g.L;
-        lc.begin();
+        lc.begin(MEMD_STAGE_OTHER);
         k_stop_stats<R><<<(unsigned)std::min<long>((g.L + 255) / 256, 1024), 256, 0, s>>>(
             (const R*)p->M, (const R*)p->amp, p->cnt, g, p->cfg.stop_sd, p->cfg.stop_sd2, p->st);
         lc.end(MEMD_STAGE_OTHER);
-        lc.begin();
+        lc.begin(MEMD_STAGE_OTHER);
         k_decide<<<1, 32, 0, s>>>(p->st, p->cnt, g, p->cfg.stop_tol, (int)p->cfg.max_iter, h_sift, p->mir);
         lc.end(MEMD_STAGE_OTHER);
-        lc.begin();
+        lc.begin(MEMD_STAGE_OTHER);
         k_apply<R, XT><<<(unsigned)std::min<size_t>((CL + 255) / 256, 4096), 256, 0, s>>>((XT*)p->X, (const R*)p->M,
                                                                                          p->st, CL);
         lc.end(MEMD_STAGE_OTHER);
@@ -403,16 +471,20 @@ static void enqueue_decomposition(memd_plan* p, cudaStream_t s, Launches& lc)
     void* const x0 = p->X;
     if (p->cum) cudaMemsetAsync(p->bnd, 0, sizeof(unsigned) * 4 * (size_t)g.C, s);
     for (int i = 0; i + 1 < nimf; ++i) {
+        nvtxRangePushA("imf");
         cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, s);
         for (int j = 0; j < maxit; ++j) {
             memd_trace_entry* tr = p->trace_dev ? p->trace_dev + ((size_t)i * (maxit + 1) + j) * (size_t)g.K * 2 : nullptr;
+            nvtxRangePushA("sift");
             enqueue_sift<P>(p, s, tr, lc);
+            nvtxRangePop();
         }
-        lc.begin();
+        nvtxRangePop();
+        lc.begin(MEMD_STAGE_OTHER);
         k_to_channel_major<XT, T><<<tg, tb, 0, s>>>((const XT*)p->X, (T*)p->imf + (size_t)i * CL, (XT*)p->run, g.C, g.L);
         lc.end(MEMD_STAGE_OTHER);
     }
-    lc.begin();
+    lc.begin(MEMD_STAGE_OTHER);
     k_to_channel_major<XT, T><<<tg, tb, 0, s>>>((const XT*)p->run, (T*)p->imf + (size_t)(nimf - 1) * CL, nullptr, g.C, g.L);
     lc.end(MEMD_STAGE_OTHER);
     if (p->X != x0) std::swap(p->X, p->Xb);  // the buffers' roles as at the start
@@ -533,6 +605,18 @@ static memd_status build_graph_stop(memd_plan* p)
     return MEMD_OK;
 }
 
+// tf32 big / small parts of the directions' high words for the tensor-core
+// projection (the directions are constant over a run).
+static void split_directions(memd_plan* p, cudaStream_t s, Launches& lc)
+{
+    if (!p->tc) return;
+    const size_t n = (size_t)p->g.K * p->Cp;
+    lc.begin(MEMD_STAGE_OTHER);
+    k_split_tf32<<<(unsigned)std::min<size_t>((n + 255) / 256, 1024), 256, 0, s>>>((const float*)p->dir, 1, p->dbig,
+                                                                                   p->dsmall, p->g.K, p->g.C, p->Cp);
+    lc.end(MEMD_STAGE_OTHER);
+}
+
 // Caller's record -> working layout; directions -> plan buffer.
 template <int P>
 static void enqueue_inputs(memd_plan* p, const typename Prec<P>::T* d_y, const typename Prec<P>::T* d_dir,
@@ -542,12 +626,14 @@ static void enqueue_inputs(memd_plan* p, const typename Prec<P>::T* d_y, const t
     using T = typename Prec<P>::T;
     const Geom& g = p->g;
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
-    lc.begin();
+    lc.begin(MEMD_STAGE_OTHER);
     k_to_sample_major<XT, T><<<tg, tb, 0, s>>>(d_y, (XT*)p->run, g.C, g.L);
     lc.end(MEMD_STAGE_OTHER);
     cudaMemcpyAsync(p->dir, d_dir, sizeof(T) * (size_t)g.K * g.C, cudaMemcpyDeviceToDevice, s);
-    if constexpr (P == MEMD_PREC_MIXED)  // float directions: the low words are zero
+    if constexpr (P == MEMD_PREC_MIXED) {  // float directions: the low words are zero
         cudaMemsetAsync((float*)p->dir + (size_t)g.K * g.C, 0, sizeof(float) * (size_t)g.K * g.C, s);
+        split_directions(p, s, lc);
+    }
 }
 
 template <int P>
@@ -575,7 +661,9 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Pre
     Launches lc;
     enqueue_inputs<P>(p, d_y, d_dir, s, lc);
     cudaEventRecord(p->e0, s);
+    nvtxRangePushA("memd_run");
     e = cudaGraphLaunch(p->exec, s);
+    nvtxRangePop();
     if (e != cudaSuccess) return set_cuda_error("run: graph launch", e);
     cudaEventRecord(p->e1, s);
     cudaMemcpyAsync(d_imfs, p->imf, sizeof(T) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
@@ -607,6 +695,7 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Pre
             for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
         }
         stats->refined = hs.pad[3];
+        stats->rechecked = hs.rechecked;
     }
     return MEMD_OK;
 }
@@ -693,8 +782,11 @@ static memd_status batched_inputs(memd_plan* p, int n, const int64_t* lengths, c
     k_batched_in<XT, T><<<dim3((unsigned)g.W, (unsigned)((C + 31) / 32)), dim3(32, 8), 0, s>>>(d_y, p->ep_yoff, (XT*)p->run,
                                                                                               C, p->ep);
     cudaMemcpyAsync(p->dir, d_dir, sizeof(T) * (size_t)g.K * C, cudaMemcpyDeviceToDevice, s);
-    if constexpr (P == MEMD_PREC_MIXED)
+    if constexpr (P == MEMD_PREC_MIXED) {
         cudaMemsetAsync((float*)p->dir + (size_t)g.K * C, 0, sizeof(float) * (size_t)g.K * C, s);
+        Launches lc;
+        split_directions(p, s, lc);
+    }
     return MEMD_OK;
 }
 
@@ -733,6 +825,7 @@ static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths,
         stats->launches = p->graph_launches + 2;
         for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
         stats->refined = hs.pad[3];
+        stats->rechecked = hs.rechecked;
     }
     return MEMD_OK;
 }
@@ -881,6 +974,7 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         return set_error(MEMD_ERR_INVALID, "plan: bad spline_end");
     if (c.boundary != MEMD_BOUNDARY_REFERENCE && c.boundary != MEMD_BOUNDARY_MIRROR)
         return set_error(MEMD_ERR_INVALID, "plan: bad boundary");
+    if (c.projection != 0 && c.projection != 1) return set_error(MEMD_ERR_INVALID, "plan: projection must be 0 or 1");
     if (c.max_epochs > 0 && (c.spline_end != MEMD_SPLINE_NATURAL || c.boundary != MEMD_BOUNDARY_REFERENCE))
         return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for natural splines and the reference boundary");
     if (c.max_epochs > 0) {
@@ -1039,12 +1133,32 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         ALLOC(p->ep_yoff, sizeof(long long) * me);
         ALLOC(p->ep.cnt, sizeof(int) * 2 * (size_t)K * me);
     }
+    // mixed form: the tensor-core projection's tf32 splits
+    p->Cp = (C + kTcKB - 1) / kTcKB * kTcKB;
+    p->tc = c.precision == MEMD_PREC_MIXED && c.projection == 0;
+    if (p->tc) {
+        p->tc_nt = std::max(16, (std::min(p->Kc, kTcMaxN) + 15) / 16 * 16);
+        ALLOC(p->xbig, sizeof(float) * (size_t)L * p->Cp);
+        ALLOC(p->xsmall, sizeof(float) * (size_t)L * p->Cp);
+        ALLOC(p->dbig, sizeof(float) * (size_t)K * p->Cp);
+        ALLOC(p->dsmall, sizeof(float) * (size_t)K * p->Cp);
+    }
     ALLOC(p->st, sizeof(RunState));
     ALLOC(p->coord_bad, sizeof(int));
 #undef ALLOC
     if (st != MEMD_OK) {
         memd_plan_destroy(p);
         return st;
+    }
+    if (p->tc) {
+        const bool mok = make_tile_map(&p->maps.xb, p->xbig, (uint64_t)p->Cp, (uint64_t)L, (uint32_t)kTcRows) &&
+                         make_tile_map(&p->maps.xs, p->xsmall, (uint64_t)p->Cp, (uint64_t)L, (uint32_t)kTcRows) &&
+                         make_tile_map(&p->maps.db, p->dbig, (uint64_t)p->Cp, (uint64_t)K, (uint32_t)p->tc_nt) &&
+                         make_tile_map(&p->maps.ds, p->dsmall, (uint64_t)p->Cp, (uint64_t)K, (uint32_t)p->tc_nt);
+        if (!mok) {
+            memd_plan_destroy(p);
+            return set_error(MEMD_ERR_CUDA, "plan: TMA descriptors (cuTensorMapEncodeTiled) could not be made");
+        }
     }
     cudaError_t e = cudaMallocHost((void**)&p->host_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);

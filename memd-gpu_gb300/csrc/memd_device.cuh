@@ -239,7 +239,9 @@ struct RunState {
     int q;                     // qualified directions of the last pass
     int trace_row;             // stop mode: trace row of the current pass (-1: none)
     int pad[4];                // [0] passes over the run, [1] sift loop continues,
-                               // [2] IMF loop continues (mirrors of the graph conditions)
+                               // [2] IMF loop continues (mirrors of the graph conditions),
+                               // [3] extremum tests re-decided in double-float
+    int rechecked;             // tensor-core projection: tests redone in FP32
 };
 
 __device__ __forceinline__ uint64_t splitmix64(uint64_t z)

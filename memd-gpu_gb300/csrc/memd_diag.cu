@@ -5,6 +5,7 @@
 
 #include "memd_device.cuh"
 #include "memd_internal.h"
+#include "memd_ptx.cuh"
 
 namespace memd {
 
@@ -54,7 +55,39 @@ static memd_status fma_rate(double* flops_per_s)
     return MEMD_OK;
 }
 
+// A wait that can never complete: an mbarrier initialised for one arrival that
+// no thread makes.  Every thread waits on it with the bounded wait of the
+// tensor-core kernels; when the limit runs out the kernel records
+// MEMD_FLAG_DEVICE_TIMEOUT and returns, and the context stays usable.
+__global__ void k_wait_timeout(int* flags, long long max_clocks)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool got = mbar_wait_bounded(&bar, 0u, max_clocks);
+    if (__syncthreads_or(!got) && threadIdx.x == 0) atomicOr(flags, MEMD_FLAG_DEVICE_TIMEOUT);
+}
+
 }  // namespace memd
+
+extern "C" memd_status memd_diag_wait_timeout(int64_t max_clocks, int32_t* flags)
+{
+    if (!flags || max_clocks < 1 || max_clocks > (1ll << 32))
+        return memd::set_error(MEMD_ERR_INVALID, "diag_wait_timeout: bad arguments");
+    int* d = nullptr;
+    if (cudaMalloc((void**)&d, sizeof(int)) != cudaSuccess) return memd::set_cuda_error("diag_wait_timeout: alloc");
+    cudaMemset(d, 0, sizeof(int));
+    memd::k_wait_timeout<<<1, 64>>>(d, (long long)max_clocks);
+    int h = 0;
+    cudaError_t e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return memd::set_cuda_error("diag_wait_timeout: run", e);
+    *flags = h;
+    return MEMD_OK;
+}
 
 extern "C" memd_status memd_diag_fma_rate(int32_t precision, double* flops_per_s)
 {

@@ -29,6 +29,8 @@ SPLINE_NATURAL, SPLINE_NOT_A_KNOT = 0, 1
 BOUNDARY_REFERENCE, BOUNDARY_MIRROR = 0, 1
 FLAG_NO_QUALIFIED_DIRECTION = 1
 FLAG_KNOT_OVERFLOW = 2
+FLAG_DEVICE_TIMEOUT = 4
+PROJ_AUTO, PROJ_CUDA_CORES = 0, 1
 
 TRACE_DTYPE = np.dtype([("count", "<i4"), ("flags", "<i4"), ("hash", "<u8")])
 
@@ -37,7 +39,7 @@ EXPORTS = [
     "memd_default_config", "memd_plan_create", "memd_plan_destroy", "memd_plan_workspace_bytes",
     "memd_plan_set_trace", "memd_run_f64", "memd_run_f32", "memd_run_batched_f64",
     "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_profile_batched_f64",
-    "memd_profile_batched_f32", "memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64", "memd_diag_fma_rate", "memd_last_error",
+    "memd_profile_batched_f32", "memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64", "memd_diag_fma_rate", "memd_diag_wait_timeout", "memd_last_error",
     "memd_version", "memd_synth_tones", "memd_synth_eeg", "memd_write_bin", "memd_bin_count",
     "memd_read_bin",
 ]
@@ -68,7 +70,7 @@ class Config(ctypes.Structure):
         ("mean_eval", ctypes.c_int32),
         ("spline_end", ctypes.c_int32),
         ("boundary", ctypes.c_int32),
-        ("reserved32", ctypes.c_int32),
+        ("projection", ctypes.c_int32),
         ("reserved", ctypes.c_int64 * 2),
     ]
 
@@ -81,7 +83,7 @@ class Stats(ctypes.Structure):
         ("launches", ctypes.c_int64),
         ("sifts", ctypes.c_int32 * 64),
         ("refined", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("rechecked", ctypes.c_int32),
     ]
 
 
@@ -138,6 +140,8 @@ def lib():
         f.restype = ctypes.c_int
     L.memd_diag_fma_rate.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     L.memd_diag_fma_rate.restype = ctypes.c_int
+    L.memd_diag_wait_timeout.argtypes = [i64, ctypes.POINTER(ctypes.c_int32)]
+    L.memd_diag_wait_timeout.restype = ctypes.c_int
     L.memd_last_error.argtypes = []
     L.memd_last_error.restype = ctypes.c_char_p
     L.memd_version.argtypes = []
@@ -292,6 +296,14 @@ def fma_rate(precision: int) -> float:
     v = ctypes.c_double()
     _check(lib().memd_diag_fma_rate(precision, ctypes.byref(v)))
     return v.value
+
+
+def wait_timeout_flags(max_clocks: int) -> int:
+    """Run the bounded-wait diagnostic (a wait nothing completes); returns the
+    run-state flags it set."""
+    v = ctypes.c_int32()
+    _check(lib().memd_diag_wait_timeout(int(max_clocks), ctypes.byref(v)))
+    return int(v.value)
 
 
 def synth_eeg(C: int, L: int, fs: float = 256.0, seed: int = 0) -> np.ndarray:

@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-epochs measurement")
     ap.add_argument("--no-long", action="store_true", help="skip the long-record measurement")
     ap.add_argument("--no-wide", action="store_true", help="skip the 128-channel record measurement")
+    ap.add_argument("--no-stop", action="store_true", help="skip the stop-criterion (8 x 2000 tones) measurement")
     return ap.parse_args()
 
 
@@ -105,6 +106,80 @@ def sum_over_ranks(x: float, device="cuda") -> float:
     """Sum of x over the ranks (x itself on one rank): the units of work that
     all replicas processed."""
     return _reduce_over_ranks(x, device, "SUM")
+
+
+def barrier():
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.barrier()
+
+
+class WallSteps:
+    """Step timer on the host clock (CPU work)."""
+
+    def __init__(self):
+        self.ms = []
+
+    def start(self):
+        self._t0 = time.perf_counter()
+
+    def stop(self):
+        self.ms.append((time.perf_counter() - self._t0) * 1e3)
+
+    def total_ms(self) -> float:
+        return float(sum(self.ms))
+
+
+class CudaSteps:
+    """Step timer from CUDA events recorded on the launching stream."""
+
+    def __init__(self, stream):
+        self.stream = stream
+        self.ev = []
+
+    def start(self):
+        import torch
+
+        self.ev.append([torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)])
+        self.ev[-1][0].record(self.stream)
+
+    def stop(self):
+        self.ev[-1][1].record(self.stream)
+
+    def total_ms(self) -> float:
+        import torch
+
+        torch.cuda.synchronize()
+        return float(sum(a.elapsed_time(b) for a, b in self.ev))
+
+
+def measure_replicated(step, units: float, steps: int, warmup: int, timer, device="cuda", sync=lambda: None,
+                       between=lambda: None) -> dict:
+    """Times `steps` calls of step() after `warmup` untimed ones, each call
+    bracketed by the timer (`between` runs outside the timed region, before
+    every timed step: the L2 flush), with a barrier and a synchronisation on
+    both sides.  Every rank is a replica working on its own data: the step
+    time is the slowest rank's, the units are summed over the ranks, and the
+    whole-job rate is units / step time."""
+    for _ in range(warmup):
+        step()
+    sync()
+    barrier()
+    sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        between()
+        timer.start()
+        step()
+        timer.stop()
+    local = timer.total_ms() / steps
+    sync()
+    wall = time.perf_counter() - t0
+    barrier()
+    ms = max_over_ranks(local, device)
+    tot = sum_over_ranks(units, device)
+    return {"ms_per_step": ms, "units": tot, "value": tot / (ms / 1e3), "wall_s": wall, "local_ms_per_step": local}
 
 
 # ----------------------------------------------------------------------------
@@ -229,36 +304,26 @@ def run_ours(args):
              ("mixed", mg.PREC_MIXED, torch.float32, {"mean_eval": 2}),
              ("mixed_direct", mg.PREC_MIXED, torch.float32, {"mean_eval": 1}),
              ("fp32", mg.PREC_F32, torch.float32, {}))
+    import memd_autotune
+
+    tuned = {}
     for name, prec, tdt, kw in FORMS:
-        plan = mg.Plan(C, L, K, NI, IT, precision=prec, **kw)
+        plan = mg.Plan(C, L, K, NI, IT, precision=prec, tuning="auto", **kw)
         plans[name] = plan
+        key = memd_autotune.config_key(plan.cfg)
+        tuned[name] = {"key": key, "choice": plan.tuning(),
+                       "source": ("autotuner (memd-gpu_gb300/tuning/gb300.json)"
+                                  if memd_autotune.lookup(plan.cfg) else "defaults (no stored choice)")}
         d = d32.to(tdt)
         dy = torch.as_tensor(y, dtype=tdt, device="cuda")
         out = torch.empty((NI, C, L), dtype=tdt, device="cuda")
-        for _ in range(args.warmup):
-            plan.run(dy, d, out, stream=stream, stats=False)
-        torch.cuda.synchronize()
-        if ws > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
         clocks = Clocks(local) if rank == 0 else None
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        t0 = time.perf_counter()
-        for i in range(args.steps):
-            flush.zero_()  # L2 flush between timed steps (256 MB > 129 MB L2)
-            ev[i][0].record(stream)
-            plan.run(dy, d, out, stream=stream, stats=False)
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        if ws > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
+        m = measure_replicated(lambda: plan.run(dy, d, out, stream=stream, stats=False), float(C * L), args.steps,
+                               args.warmup, CudaSteps(stream), sync=torch.cuda.synchronize,
+                               between=flush.zero_)  # L2 flush between timed steps (256 MB > 129 MB L2)
         ck = clocks.stop() if clocks else None
-        ms = [a.elapsed_time(b) for a, b in ev]
-        tot = max_over_ranks(sum(ms))
         st = plan.run(dy, d, out, stats=True)
-        results[name] = {"ms_per_step": tot / args.steps, "wall_s": wall, "clocks": ck,
+        results[name] = {"ms_per_step": m["ms_per_step"], "wall_s": m["wall_s"], "clocks": ck,
                          "launches_per_step": int(st.launches), "flags": int(st.flags), "refined": int(st.refined),
                          "workspace_gb": plan.workspace_bytes / 1e9}
         outs[name] = (out, d, dy)
@@ -281,22 +346,14 @@ def run_ours(args):
     dy = torch.empty((C, L), dtype=tdt, device="cuda")
     dout = torch.empty((NI, C, L), dtype=tdt, device="cuda")
     d = outs[head][1]
-    for _ in range(2):
+
+    def e2e_step():
         dy.copy_(hy, non_blocking=True)
         plan.run(dy, d, dout, stream=stream, stats=False)
         hout.copy_(dout, non_blocking=True)
-    torch.cuda.synchronize()
-    if ws > 1:
-        dist.barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for i in range(args.steps):
-        dy.copy_(hy, non_blocking=True)
-        plan.run(dy, d, dout, stream=stream, stats=False)
-        hout.copy_(dout, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+
+    e2e_ms = measure_replicated(e2e_step, float(C * L), args.steps, max(args.warmup, 2), CudaSteps(stream),
+                                sync=torch.cuda.synchronize, between=flush.zero_)["ms_per_step"]
     elem = 8 if head == "fp64" else 4
 
     # per-stage timing (eager, every kernel bracketed by CUDA events) and knot
@@ -408,6 +465,7 @@ def run_ours(args):
                     "h2d_bytes_per_step": C * L * elem, "d2h_bytes_per_step": NI * C * L * elem,
                     "ms_per_step": e2e_ms, "api": "memd_run_f32/f64 (C ABI) via ctypes"},
             "gpu_launches": results[head]["launches_per_step"] * args.steps,
+            "tuning": tuned,
             "roofline": roofline(head),
             "roofline_by_form": {n: roofline(n) for n in NAMES},
             "fma_rate_tflops": fma,
@@ -424,6 +482,13 @@ def run_ours(args):
         bres = batched_epochs(rank)
         if rank == 0:
             line["batched_epochs"] = bres
+    if not args.no_stop:
+        for p in plans.values():
+            p.close()
+        plans = {}
+        sres = stop_criterion(rank, args)
+        if rank == 0:
+            line["stop_criterion"] = sres
     if not args.no_wide:
         for p in plans.values():
             p.close()
@@ -479,24 +544,18 @@ def batched_epochs(rank):
     outs = {}
     stream = torch.cuda.current_stream()
     for name, prec, tdt in (("mixed", mg.PREC_MIXED, torch.float32), ("fp64", mg.PREC_F64, torch.float64)):
-        plan = mg.Plan(C, B["Lmax"], K, NI, IT, precision=prec, max_epochs=B["epochs"])
+        plan = mg.Plan(C, B["Lmax"], K, NI, IT, precision=prec, max_epochs=B["epochs"], tuning="auto")
         y = torch.as_tensor(flat, dtype=tdt, device="cuda")
         o = torch.empty(NI * y.numel(), dtype=tdt, device="cuda")
         d = d32.to(tdt)
-        for _ in range(B["warmup"]):
-            plan.run_batched(y, lengths, offs, d, o, stream=stream, stats=False)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(B["steps"]):
-            plan.run_batched(y, lengths, offs, d, o, stream=stream, stats=False)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = max_over_ranks(e0.elapsed_time(e1) / B["steps"])
+        # every replica decomposes its own epoch set
+        m = measure_replicated(lambda: plan.run_batched(y, lengths, offs, d, o, stream=stream, stats=False),
+                               C * float(lengths.sum()), B["steps"], B["warmup"], CudaSteps(stream),
+                               sync=torch.cuda.synchronize)
+        ms = m["ms_per_step"]
         st = plan.run_batched(y, lengths, offs, d, o)
-        units = sum_over_ranks(C * float(lengths.sum()))  # every replica decomposes its own epoch set
-        out[name] = {"ms_per_step": ms, "channel_samples_per_s": units / (ms / 1e3),
-                     "workspace_gb": plan.workspace_bytes / 1e9, "flags": int(st.flags)}
+        out[name] = {"ms_per_step": ms, "channel_samples_per_s": m["value"],
+                     "workspace_gb": plan.workspace_bytes / 1e9, "flags": int(st.flags), "tuning": plan.tuning()}
         outs[name] = o.cpu().numpy().astype(np.float64)
         plan.close()
         del y, o
@@ -508,6 +567,51 @@ def batched_epochs(rank):
         for i in range(NI):
             worst = max(worst, rel_l2(a[i], b[i]))
     out["precision_gate"] = {"max_rel_l2_per_imf_vs_fp64": worst, "passed": worst <= GATE}
+    out["mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    return out
+
+
+# stop criterion: 8 channels x 2,000 samples (fs 1 kHz) of tones at 5, 20 and
+# 60 Hz with noise (seed 0), 64 directions, thresholds (0.075, 0.75, 0.075),
+# up to 10 IMFs plus the residual, at most 200 sifts per IMF
+STOP = dict(workload="tones8_2000_k64_stop", C=8, L=2000, K=64, num_imfs=11, max_iter=200, fs=1000.0,
+            sd=0.075, sd2=0.75, tol=0.075)
+
+
+def stop_criterion(rank, args):
+    """Decomposition time of the FP64 and mixed forms in stop mode (nested
+    conditional graph loops, no host round trip), their IMF and sift counts,
+    and the mixed form's per-IMF error against FP64."""
+    import torch
+
+    import memd_gb300 as mg
+
+    S = STOP
+    C, L, K, NI, IT = S["C"], S["L"], S["K"], S["num_imfs"], S["max_iter"]
+    y = memd_signals.as_float32_record(memd_signals.tones(C, L, S["fs"], seed=rank))
+    d32 = mg.directions(C, K, dtype="f32")
+    stream = torch.cuda.current_stream()
+    out = {"workload": S["workload"], "C": C, "L": L, "K": K, "max_imfs": NI - 1, "max_iter": IT,
+           "thresholds": [S["sd"], S["sd2"], S["tol"]]}
+    res = {}
+    for name, prec, tdt in (("fp64", mg.PREC_F64, torch.float64), ("mixed", mg.PREC_MIXED, torch.float32)):
+        plan = mg.Plan(C, L, K, NI, IT, precision=prec, stop_mode=mg.STOP_CRITERION, stop_sd=S["sd"],
+                       stop_sd2=S["sd2"], stop_tol=S["tol"])
+        dy = torch.as_tensor(y, dtype=tdt, device="cuda")
+        o = torch.empty((NI, C, L), dtype=tdt, device="cuda")
+        d = d32.to(tdt)
+        m = measure_replicated(lambda: plan.run(dy, d, o, stream=stream, stats=False), float(C * L),
+                               max(args.steps, 5), max(args.warmup, 3), CudaSteps(stream), sync=torch.cuda.synchronize)
+        st = plan.run(dy, d, o)
+        sifts = [int(v) for v in st.sifts[: st.n_imfs]]
+        out[name] = {"ms_per_step": m["ms_per_step"], "channel_samples_per_s": m["value"], "n_imfs": int(st.n_imfs),
+                     "sifts": sifts, "sift_iters_per_s": sum(sifts) / (m["ms_per_step"] / 1e3),
+                     "flags": int(st.flags)}
+        res[name] = o.cpu().numpy().astype(np.float64)
+        plan.close()
+    rl = [rel_l2(res["mixed"][i], res["fp64"][i]) for i in range(NI) if np.linalg.norm(res["fp64"][i]) > 0]
+    out["precision_gate"] = {"rel_l2_per_imf_vs_fp64": rl, "max": max(rl), "passed": max(rl) <= GATE,
+                             "same_imf_and_sift_counts": out["mixed"]["sifts"] == out["fp64"]["sifts"]}
     out["mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
     return out
 
@@ -538,22 +642,15 @@ def single_record(rank, Lr):
     out = {"workload": Lr["workload"], "C": C, "L": L, "K": K, "num_imfs": NI, "max_iter": IT}
     res = {}
     for name, prec, tdt in (("mixed", mg.PREC_MIXED, torch.float32), ("fp64", mg.PREC_F64, torch.float64)):
-        plan = mg.Plan(C, L, K, NI, IT, precision=prec)
+        plan = mg.Plan(C, L, K, NI, IT, precision=prec, tuning="auto")
         dy = torch.as_tensor(y, dtype=tdt, device="cuda")
         o = torch.empty((NI, C, L), dtype=tdt, device="cuda")
         d = d32.to(tdt)
-        for _ in range(Lr["warmup"]):
-            plan.run(dy, d, o, stream=stream, stats=False)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(Lr["steps"]):
-            plan.run(dy, d, o, stream=stream, stats=False)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms = max_over_ranks(e0.elapsed_time(e1) / Lr["steps"])
+        m = measure_replicated(lambda: plan.run(dy, d, o, stream=stream, stats=False), float(C * L), Lr["steps"],
+                               Lr["warmup"], CudaSteps(stream), sync=torch.cuda.synchronize)
+        ms = m["ms_per_step"]
         st = plan.run(dy, d, o)
-        entry = {"ms_per_step": ms, "channel_samples_per_s": sum_over_ranks(C * L) / (ms / 1e3),
+        entry = {"ms_per_step": ms, "channel_samples_per_s": m["value"],
                  "workspace_gb": plan.workspace_bytes / 1e9, "flags": int(st.flags)}
         if name == "mixed":
             plan.set_trace(True)

@@ -136,9 +136,7 @@ typedef struct {
     int32_t refined;       /* mixed precision: extremum tests re-decided in
                               double-float because the FP32 margin was within
                               the projection's error bound */
-    int32_t rechecked;     /* mixed precision, tensor-core projection: tests
-                              redone with FP32 dot products because the
-                              tensor-core margin was within its bound */
+    int32_t reserved;
 } memd_stats;
 
 /* Per-stage device time of one eagerly launched decomposition (every kernel
@@ -163,6 +161,9 @@ typedef struct {
 #define MEMD_FLAG_DEVICE_TIMEOUT 4          /* a bounded device-side wait ran out (a kernel
                                                gave up on a copy or product it issued);
                                                the run's results are not valid */
+#define MEMD_FLAG_CHECK_FAILED 8            /* bounds-checked build (libmemd_gb300_checked.so):
+                                               an index check failed and its access was
+                                               skipped */
 
 /* One entry per (IMF, sift, direction, envelope) when a trace buffer is
  * given: the extrema index set of that projected direction. */
@@ -174,10 +175,32 @@ typedef struct {
 
 typedef struct memd_plan memd_plan;
 
+/* Launch shapes of a plan's kernels (what the autotuner chooses; 0 = the
+ * default).  None of them changes what is computed beyond rounding: segment
+ * lengths only move where the windowed tridiagonal sweeps start (their
+ * truncation is below the arithmetic's precision), the rest are grid
+ * shapes and work distribution. */
+typedef struct {
+    int32_t solve_segment;      /* longest substitution segment in knots, a power of two in [32, 1024] (256) */
+    int32_t solve_min_segment;  /* shortest substitution segment, a power of two in [16, solve_segment] (64) */
+    int32_t factor_segment;     /* factorisation rows per thread, 4 .. 256 (FP64 64, otherwise 16) */
+    int32_t solve_queue;        /* substitution work: 1 = device work queue pulled by a persistent grid,
+                                   2 or 0 = one warp per possible segment (the default) */
+    int32_t mean_ctas;          /* impulse-accumulation mean: CTAs the split of spans over CTAs aims for,
+                                   128 .. 65536 (2048) */
+    int32_t proj_tile_n;        /* tensor-core projection: directions per tile, a multiple of 16 in
+                                   [16, 256] (64) */
+    int32_t reserved[10];
+} memd_tuning;
+
 void memd_default_config(memd_config* cfg);
 
 /* Allocates every device buffer the runs need (nothing is allocated later). */
 memd_status memd_plan_create(const memd_config* cfg, memd_plan** plan);
+/* memd_plan_create with explicit launch shapes (tuning may be NULL: defaults). */
+memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tuning, memd_plan** plan);
+/* The launch shapes a plan uses (the defaults filled in). */
+memd_status memd_plan_get_tuning(const memd_plan* plan, memd_tuning* tuning);
 memd_status memd_plan_destroy(memd_plan* plan);
 /* Device bytes held by the plan. */
 size_t memd_plan_workspace_bytes(const memd_plan* plan);

@@ -18,6 +18,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libmemd_gb300.so")
+# the same library with the index checks of MEMD_CHECKED compiled in (tests)
+LIB_CHECKED = os.path.join(LIBDIR, "libmemd_gb300_checked.so")
 INCLUDE = os.path.join(REPO, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -53,12 +55,12 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src: str, extra_deps: list[str]) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(src: str, extra_deps: list[str], checked: bool = False) -> str:
+    obj = os.path.join(BUILD, os.path.basename(src) + (".checked.o" if checked else ".o"))
     if _newer(obj, [src] + extra_deps):
         return obj
     if src.endswith(".cu"):
-        cmd = [_nvcc()] + NVFLAGS + ["-c", src, "-o", obj]
+        cmd = [_nvcc()] + NVFLAGS + (["-DMEMD_CHECKED"] if checked else []) + ["-c", src, "-o", obj]
     else:
         cmd = ["g++"] + CXXFLAGS + ["-c", src, "-o", obj]
     subprocess.check_call(cmd)
@@ -110,10 +112,17 @@ def build(verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     deps = _headers()
     srcs = [os.path.join(CSRC, s) for s in CU_SOURCES + CXX_SOURCES]
-    with cf.ThreadPoolExecutor(max_workers=max(2, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, deps), srcs))
+    api = os.path.join(CSRC, "memd_api.cu")
+    jobs = [(s_, False) for s_ in srcs] + [(api, True)]
+    with cf.ThreadPoolExecutor(max_workers=max(2, len(jobs))) as ex:
+        built = list(ex.map(lambda j: _compile(j[0], deps, j[1]), jobs))
+    objs, api_checked = built[:-1], built[-1]
     if not _newer(LIB, objs):
         cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        subprocess.check_call(cmd)
+    objs_checked = [api_checked if o.endswith("memd_api.cu.o") else o for o in objs]
+    if not _newer(LIB_CHECKED, objs_checked):
+        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB_CHECKED] + objs_checked + ["-lcudart"]
         subprocess.check_call(cmd)
     build_host_tools()
     if verbose:

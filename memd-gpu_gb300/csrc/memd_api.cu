@@ -123,6 +123,11 @@ struct memd_plan {
     float* dbig;
     float* dsmall;
     memd::TcMaps maps;
+    // substitution work queue (persistent sweeps pull segments by ticket)
+    int squeue;       // 1: queue, 0: one warp per possible segment
+    memd::SolveQueue sq;
+    int sms;          // multiprocessors of the device
+    int cum_ctas;     // impulse-accumulation mean: working CTAs the split of spans over CTAs aims for
 };
 
 namespace memd {
@@ -175,6 +180,16 @@ static bool make_tile_map(CUtensorMap* m, void* base, uint64_t cols, uint64_t ro
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
            CUDA_SUCCESS;
+}
+
+// Grid of a persistent kernel: as many CTAs as can be resident at once (at
+// most the static grid).
+template <typename Kern>
+static unsigned persistent_grid(Kern kern, int threads, int sms, unsigned nb_static)
+{
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, 0) != cudaSuccess || occ < 1) occ = 1;
+    return std::min<unsigned>(nb_static, (unsigned)std::max(1, sms * occ));
 }
 
 // ----- launch accounting / per-stage timing --------------------------------
@@ -340,14 +355,14 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.begin(MEMD_STAGE_PROJECT);
         if constexpr (P == MEMD_PREC_MIXED) {
             if (p->tc) {
-                if (ch == 0) {  // the signal's tf32 split, once per sift
+                if (ch == 0) {  // tf32 split of the signal's first differences, once per sift
                     const size_t n = (size_t)g.L * p->Cp;
                     k_split_tf32<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(
-                        (const float*)p->X, 2, p->xbig, p->xsmall, g.L, g.C, p->Cp);
+                        p->X, 1, p->xbig, p->xsmall, g.L, g.C, p->Cp);
                     lc.end(MEMD_STAGE_PROJECT);
                     lc.begin(MEMD_STAGE_PROJECT);
                 }
-                dim3 tg((unsigned)((g.L + kTcRows - 1) / kTcRows), (unsigned)((kc + kTcMaxN - 1) / kTcMaxN));
+                dim3 tg((unsigned)((g.L + kTcRows - 1) / kTcRows), (unsigned)((kc + p->tc_nt - 1) / p->tc_nt));
                 k_project_tc<<<tg, kTcThreads, tc_smem_bytes(p->tc_nt), s>>>(
                     p->maps, (const float2*)p->X, (const float*)p->dir, (const float*)p->dir + (size_t)g.K * g.C,
                     p->bits, g, k0, kc, p->Cp, p->tc_nt, p->st, p->ep);
@@ -389,22 +404,31 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         if (g.nak)
             k_factor<R, true><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
                                                                        (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
-                                                                       p->cum ? p->cumcfg : nullptr, p->ep);
+                                                                       p->cum ? p->cumcfg : nullptr, p->ep, p->cum_ctas);
         else
             k_factor<R, false><<<(unsigned)((nf + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, (const R*)p->rtab,
                                                                         (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
-                                                                        p->cum ? p->cumcfg : nullptr, p->ep);
+                                                                        p->cum ? p->cumcfg : nullptr, p->ep, p->cum_ctas);
         lc.end(MEMD_STAGE_FACTOR);
         const long nseg = (p->H < 0) ? 1 : (g.cap + p->Ss - 1) / p->Ss;
         const long ns = 2L * kc * nseg * p->ngroups * 32;
         const unsigned nb = (unsigned)((ns + kSolveThreads - 1) / kSolveThreads);
         unsigned* bcur = p->cum ? p->bnd + (size_t)(p->bpass & 1) * 2 * g.C : nullptr;
+        SolveQueue q{};  // null prefix: the static mapping
+        if (p->squeue) {
+            q = p->sq;
+            lc.begin(MEMD_STAGE_SOLVE);
+            k_solve_queue<<<1, 1024, 0, s>>>(p->cnt, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, q);
+            lc.end(MEMD_STAGE_SOLVE);
+        }
         lc.begin(MEMD_STAGE_SOLVE);
         bool xm = false;
 #define MEMD_FWD(XM_, EPB_, NAK_)                                                                               \
-    k_solve_fwd<R, XT, XM_, EPB_, NAK_><<<nb, kSolveThreads, 0, s>>>(                                          \
+    k_solve_fwd<R, XT, XM_, EPB_, NAK_><<<p->squeue ? persistent_grid(k_solve_fwd<R, XT, XM_, EPB_, NAK_>,     \
+                                                                      kSolveThreads, p->sms, nb) : nb,          \
+                                          kSolveThreads, 0, s>>>(                                              \
         (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, \
-        bcur, XM_ ? (const XT*)p->X : nullptr, p->knots, XM_ ? (const R*)p->yend : nullptr, p->ep)
+        bcur, XM_ ? (const XT*)p->X : nullptr, p->knots, XM_ ? (const R*)p->yend : nullptr, p->ep, q)
         if constexpr (P == MEMD_PREC_MIXED) {
             if (p->cum) {  // knot values from the working signal (the impulse-accumulation path)
                 xm = true;
@@ -421,13 +445,15 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin(MEMD_STAGE_SOLVE);
         if (g.nak)
-            k_solve_bwd<R, true><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
-                                                             (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
-                                                             p->knots);
+            k_solve_bwd<R, true><<<p->squeue ? persistent_grid(k_solve_bwd<R, true>, kSolveThreads, p->sms, nb) : nb,
+                                   kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
+                                                          (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
+                                                          p->knots, q);
         else
-            k_solve_bwd<R, false><<<nb, kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
-                                                              (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
-                                                              p->knots);
+            k_solve_bwd<R, false><<<p->squeue ? persistent_grid(k_solve_bwd<R, false>, kSolveThreads, p->sms, nb) : nb,
+                                    kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
+                                                           (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
+                                                           p->knots, q);
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin(MEMD_STAGE_EVAL);
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
@@ -612,9 +638,25 @@ static void split_directions(memd_plan* p, cudaStream_t s, Launches& lc)
     if (!p->tc) return;
     const size_t n = (size_t)p->g.K * p->Cp;
     lc.begin(MEMD_STAGE_OTHER);
-    k_split_tf32<<<(unsigned)std::min<size_t>((n + 255) / 256, 1024), 256, 0, s>>>((const float*)p->dir, 1, p->dbig,
-                                                                                   p->dsmall, p->g.K, p->g.C, p->Cp);
+    k_split_tf32<<<(unsigned)std::min<size_t>((n + 255) / 256, 1024), 256, 0, s>>>(p->dir, 0, p->dbig, p->dsmall,
+                                                                                   p->g.K, p->g.C, p->Cp);
     lc.end(MEMD_STAGE_OTHER);
+}
+
+// Bounds-checked build: the index-check failures since the last call
+// (MEMD_FLAG_CHECK_FAILED), cleared; always 0 in the normal build.
+static int checked_flags()
+{
+#ifdef MEMD_CHECKED
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_memd_check, sizeof(int)) != cudaSuccess) return 0;
+    if (v) {
+        const int z = 0;
+        cudaMemcpyToSymbol(g_memd_check, &z, sizeof(int));
+        return MEMD_FLAG_CHECK_FAILED;
+    }
+#endif
+    return 0;
 }
 
 // Caller's record -> working layout; directions -> plan buffer.
@@ -683,7 +725,7 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Pre
         cudaEventElapsedTime(&ms, p->e0, p->e1);
         memset(stats, 0, sizeof(*stats));
         stats->elapsed_ms = ms;
-        stats->flags = hs.flags;
+        stats->flags = hs.flags | checked_flags();
         if (stopm) {
             stats->n_imfs = hs.n_imfs;
             for (int i = 0; i < hs.n_imfs && i < 64; ++i) stats->sifts[i] = hs.sifts[i];
@@ -695,7 +737,6 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Pre
             for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
         }
         stats->refined = hs.pad[3];
-        stats->rechecked = hs.rechecked;
     }
     return MEMD_OK;
 }
@@ -820,12 +861,11 @@ static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths,
         cudaEventElapsedTime(&ms, p->e0, p->e1);
         memset(stats, 0, sizeof(*stats));
         stats->elapsed_ms = ms;
-        stats->flags = hs.flags;
+        stats->flags = hs.flags | checked_flags();
         stats->n_imfs = (int)p->cfg.num_imfs - 1;
         stats->launches = p->graph_launches + 2;
         for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
         stats->refined = hs.pad[3];
-        stats->rechecked = hs.rechecked;
     }
     return MEMD_OK;
 }
@@ -936,7 +976,11 @@ void memd_default_config(memd_config* cfg)
 
 const char* memd_last_error(void) { return memd::g_err.c_str(); }
 
-const char* memd_version(void) { return "memd-gb300 0.1 (sm_103a)"; }
+#ifdef MEMD_CHECKED
+const char* memd_version(void) { return "memd-gb300 0.2 (sm_103a, bounds-checked)"; }
+#else
+const char* memd_version(void) { return "memd-gb300 0.2 (sm_103a)"; }
+#endif
 
 memd_status memd_plan_destroy(memd_plan* p)
 {
@@ -953,10 +997,43 @@ memd_status memd_plan_destroy(memd_plan* p)
 
 size_t memd_plan_workspace_bytes(const memd_plan* p) { return p ? p->bytes : 0; }
 
-memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
+memd_status memd_plan_create(const memd_config* cfg, memd_plan** out) { return memd_plan_create_tuned(cfg, nullptr, out); }
+
+memd_status memd_plan_get_tuning(const memd_plan* p, memd_tuning* t)
+{
+    using namespace memd;
+    if (!p || !t) return set_error(MEMD_ERR_INVALID, "get_tuning: null argument");
+    memset(t, 0, sizeof(*t));
+    t->solve_segment = p->S;
+    t->solve_min_segment = p->Ss;
+    t->factor_segment = p->Sf;
+    t->solve_queue = p->squeue ? 1 : 2;
+    t->mean_ctas = p->cum_ctas;
+    t->proj_tile_n = p->tc ? p->tc_nt : 0;
+    return MEMD_OK;
+}
+
+memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tun, memd_plan** out)
 {
     using namespace memd;
     if (!cfg || !out) return set_error(MEMD_ERR_INVALID, "plan: null argument");
+    memd_tuning tu;
+    memset(&tu, 0, sizeof(tu));
+    if (tun) tu = *tun;
+    auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+    if (tu.solve_segment && (!pow2(tu.solve_segment) || tu.solve_segment < 32 || tu.solve_segment > 1024))
+        return set_error(MEMD_ERR_INVALID, "tuning: solve_segment must be a power of two in [32, 1024]");
+    if (tu.solve_min_segment &&
+        (!pow2(tu.solve_min_segment) || tu.solve_min_segment < 16 ||
+         tu.solve_min_segment > (tu.solve_segment ? tu.solve_segment : 256)))
+        return set_error(MEMD_ERR_INVALID, "tuning: solve_min_segment must be a power of two in [16, solve_segment]");
+    if (tu.factor_segment && (tu.factor_segment < 4 || tu.factor_segment > 256))
+        return set_error(MEMD_ERR_INVALID, "tuning: factor_segment must be in [4, 256]");
+    if (tu.solve_queue < 0 || tu.solve_queue > 2) return set_error(MEMD_ERR_INVALID, "tuning: solve_queue must be 0, 1 or 2");
+    if (tu.mean_ctas && (tu.mean_ctas < 128 || tu.mean_ctas > 65536))
+        return set_error(MEMD_ERR_INVALID, "tuning: mean_ctas must be in [128, 65536]");
+    if (tu.proj_tile_n && (tu.proj_tile_n % 16 != 0 || tu.proj_tile_n < 16 || tu.proj_tile_n > kTcMaxN))
+        return set_error(MEMD_ERR_INVALID, "tuning: proj_tile_n must be a multiple of 16 in [16, 256]");
     *out = nullptr;
     const memd_config c = *cfg;
     if (c.channels < 1 || c.channels > 256) return set_error(MEMD_ERR_INVALID, "plan: channels must be in [1, 256]");
@@ -1027,12 +1104,12 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
         // halo lengths: the truncation error decays by <= 1/2 (solve) and
         // <= 1/3 (pivots) per knot; FP64 and double-float need ~1e-15
         const bool wide = f64 || c.precision == MEMD_PREC_MIXED;
-        p->S = 256;
-        p->Ss = 64;
+        p->S = tu.solve_segment ? tu.solve_segment : 256;
+        p->Ss = tu.solve_min_segment ? tu.solve_min_segment : std::min(64, p->S);
         p->H = c.solve_window > 0 ? (int)c.solve_window : (f64 ? 48 : (wide ? 32 : 24));
         // short factorisation segments (the pivot recurrence is latency-bound),
         // except for FP64, whose longer halo would dominate
-        p->Sf = f64 ? 64 : 16;
+        p->Sf = tu.factor_segment ? tu.factor_segment : (f64 ? 64 : 16);
         p->Hf = f64 ? 40 : (wide ? 32 : 20);
     }
     p->GS = 32;  // solve: one warp per (envelope, direction, segment, 32 channels)
@@ -1137,11 +1214,20 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
     p->Cp = (C + kTcKB - 1) / kTcKB * kTcKB;
     p->tc = c.precision == MEMD_PREC_MIXED && c.projection == 0;
     if (p->tc) {
-        p->tc_nt = std::max(16, (std::min(p->Kc, kTcMaxN) + 15) / 16 * 16);
+        // directions per tile: 64 by default (more, narrower tiles keep more
+        // CTAs in flight; the kernel is latency-bound, not tensor-bound)
+        p->tc_nt = std::max(16, (std::min(p->Kc, tu.proj_tile_n ? tu.proj_tile_n : 64) + 15) / 16 * 16);
         ALLOC(p->xbig, sizeof(float) * (size_t)L * p->Cp);
         ALLOC(p->xsmall, sizeof(float) * (size_t)L * p->Cp);
         ALLOC(p->dbig, sizeof(float) * (size_t)K * p->Cp);
         ALLOC(p->dsmall, sizeof(float) * (size_t)K * p->Cp);
+    }
+    p->squeue = tu.solve_queue == 1;
+    p->cum_ctas = tu.mean_ctas ? tu.mean_ctas : 2048;
+    if (p->squeue) {
+        ALLOC(p->sq.pref, sizeof(int) * (2 * Kc + 1));
+        ALLOC(p->sq.total, sizeof(int));
+        ALLOC(p->sq.ticket, sizeof(int) * 2);
     }
     ALLOC(p->st, sizeof(RunState));
     ALLOC(p->coord_bad, sizeof(int));
@@ -1159,6 +1245,13 @@ memd_status memd_plan_create(const memd_config* cfg, memd_plan** out)
             memd_plan_destroy(p);
             return set_error(MEMD_ERR_CUDA, "plan: TMA descriptors (cuTensorMapEncodeTiled) could not be made");
         }
+    }
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        p->sms = 0;
+        cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
+        if (p->sms < 1) p->sms = 1;
     }
     cudaError_t e = cudaMallocHost((void**)&p->host_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);

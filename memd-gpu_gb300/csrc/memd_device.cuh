@@ -225,6 +225,23 @@ __device__ __forceinline__ bool dir_qualifies(const Geom& g, const Epochs& ep, c
 constexpr int kMirWords = 16;
 enum { kMirLsym = 0, kMirRsym = 1, kMirNl = 2, kMirNr = 4, kMirLsrc = 6, kMirRsrc = 10 };
 
+// Bounds-checked build (-DMEMD_CHECKED): MEMD_CHECK(cond) is false when an
+// index check fails, which also records the failure in g_memd_check (read and
+// cleared by the host after each run, reported as MEMD_FLAG_CHECK_FAILED); the
+// guarded access is then skipped instead of touching memory out of bounds.
+// In the normal build the checks compile away.
+#ifdef MEMD_CHECKED
+__device__ int g_memd_check;
+__device__ __forceinline__ bool memd_check(bool ok)
+{
+    if (!ok) atomicOr(&g_memd_check, 1);
+    return ok;
+}
+#define MEMD_CHECK(cond) memd::memd_check((cond))
+#else
+#define MEMD_CHECK(cond) true
+#endif
+
 // Per-run device state (counters and sticky flags).
 struct RunState {
     int flags;                 // MEMD_FLAG_* bits
@@ -241,7 +258,6 @@ struct RunState {
     int pad[4];                // [0] passes over the run, [1] sift loop continues,
                                // [2] IMF loop continues (mirrors of the graph conditions),
                                // [3] extremum tests re-decided in double-float
-    int rechecked;             // tensor-core projection: tests redone in FP32
 };
 
 __device__ __forceinline__ uint64_t splitmix64(uint64_t z)

@@ -376,7 +376,7 @@ template <typename real, bool NAK>
 __global__ void __launch_bounds__(128)
 k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real* __restrict__ rtab,
          Fac<real>* __restrict__ fac, Geom g, int k0, int Kc, int Sf, int Hf, int* __restrict__ cumcfg,
-         Epochs ep)
+         Epochs ep, int cum_ctas)
 {
     // cumcfg != nullptr (impulse-accumulation mean): block 0 picks the mean
     // kernel's anchor span, 32 m samples (m the largest power of two <= 4 with
@@ -403,12 +403,12 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
                 while (m < kCumMaxWords && 32.0 * (2 * m) <= 2.0 * h) m *= 2;
             }
             // parts per span: the fewest (a power of two <= m) that still give
-            // the launch ~2048 working CTAs; a long record or a batch has
-            // enough spans on its own, and every extra part costs a flush of
-            // the span's accumulators
+            // the launch ~cum_ctas working CTAs (2048 unless tuned); a long
+            // record or a batch has enough spans on its own, and every extra
+            // part costs a flush of the span's accumulators
             const long spans = (long)((g.W + m - 1) / m) * ((g.C + 31) / 32);
             int P = m;
-            while (P > 1 && spans * (P / 2) >= 2048) P >>= 1;
+            while (P > 1 && spans * (P / 2) >= cum_ctas) P >>= 1;
             cumcfg[0] = m;
             cumcfg[1] = P;
         }
@@ -526,36 +526,145 @@ struct SolveItem {
     bool ok;
 };
 
-__device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, int k0, int Kc, int S, int Ss, int H,
-                                                int ngroups)
+// Segment length of a system of E knots: the longest power of two in [Ss, S]
+// that still gives it more than 16 segments (H < 0: one window over all).
+__device__ __forceinline__ int solve_seg_len(int E, int cap, int S, int Ss, int H)
+{
+    if (H < 0) return cap;
+    for (int t = S; t > Ss; t >>= 1)
+        if (E > 16 * t) return t;
+    return Ss;
+}
+
+// Device work queue of the substitution (optional, memd_tuning.solve_queue):
+// k_solve_queue writes, per pass, the segments before each (envelope,
+// direction) slot; the persistent sweeps take items (segment x channel group)
+// by atomic ticket until the pass runs out.  Without it (pref == nullptr)
+// warp w of the launch is item w, over every segment the capacity allows.
+struct SolveQueue {
+    int* pref;    // [2 Kc + 1] segments before slot s (pref[2 Kc] = all segments)
+    int* total;   // [1] items: segments x channel groups
+    int* ticket;  // [2] next item of the forward and of the backward sweep
+};
+
+__device__ __forceinline__ SolveItem solve_item_of(int env, int kk, int seg, int cgi, const int* cnt, const Geom& g,
+                                                   int k0, int S, int Ss, int H)
 {
     SolveItem it;
-    const long gw = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp = item
-    const int cgi = (int)(gw % ngroups);
-    const long item = gw / ngroups;
-    const int slot = (int)(item % (2 * Kc));
-    it.seg = (int)(item / (2 * Kc));
-    it.env = slot / Kc;
-    it.kk = slot - it.env * Kc;
+    it.seg = seg;
+    it.env = env;
+    it.kk = kk;
     it.c = cgi * 32 + (int)(threadIdx.x & 31);
     it.ok = false;
-    it.E = cnt[it.env * g.K + k0 + it.kk];
+    it.E = cnt[env * g.K + k0 + kk];
     if (it.E > g.cap || it.E < 2) return it;
-    // the longest power-of-two segment in [Ss, S] that still gives each
-    // system more than 16 segments
-    int Se = Ss;
-    if (H < 0) Se = g.cap;
-    else
-        for (int t = S; t > Ss; t >>= 1)
-            if (it.E > 16 * t) {
-                Se = t;
-                break;
-            }
-    it.i0 = it.seg * Se;
+    const int Se = solve_seg_len(it.E, g.cap, S, Ss, H);
+    it.i0 = seg * Se;
     if (it.i0 >= it.E) return it;
     it.i1 = min(it.E, it.i0 + Se);
     it.ok = true;
     return it;
+}
+
+// static mapping: warp w of the launch = item w (segments up to the capacity;
+// those past a system's knots exit)
+__device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, int k0, int Kc, int S, int Ss, int H,
+                                                int ngroups)
+{
+    const long gw = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp = item
+    const int cgi = (int)(gw % ngroups);
+    const long item = gw / ngroups;
+    const int slot = (int)(item % (2 * Kc));
+    const int seg = (int)(item / (2 * Kc));
+    return solve_item_of(slot / Kc, slot % Kc, seg, cgi, cnt, g, k0, S, Ss, H);
+}
+
+// queue mapping: item = segment index over all slots x channel group; the
+// slot by binary search in the prefix
+__device__ __forceinline__ SolveItem solve_item_queued(int item, const SolveQueue& q, const int* cnt, const Geom& g,
+                                                       int k0, int Kc, int S, int Ss, int H, int ngroups)
+{
+    const int cgi = item % ngroups;
+    const int si = item / ngroups;
+    int lo = 0, hi = 2 * Kc;  // pref[lo] <= si < pref[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&q.pref[mid]) <= si) lo = mid;
+        else hi = mid;
+    }
+    return solve_item_of(lo / Kc, lo % Kc, si - __ldg(&q.pref[lo]), cgi, cnt, g, k0, S, Ss, H);
+}
+
+// The next item of this warp: the static mapping (one item, q.pref == nullptr)
+// or the queue's next ticket; false when there is none.
+__device__ __forceinline__ bool solve_next(SolveItem& it, bool& first, int which, const SolveQueue& q, const int* cnt,
+                                           const Geom& g, int k0, int Kc, int S, int Ss, int H, int ngroups)
+{
+    if (!q.pref) {
+        if (!first) return false;
+        first = false;
+        it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
+        return true;
+    }
+    int item = 0;
+    if ((threadIdx.x & 31) == 0) item = atomicAdd(&q.ticket[which], 1);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= __ldcg(q.total)) return false;
+    it = solve_item_queued(item, q, cnt, g, k0, Kc, S, Ss, H, ngroups);
+    return true;
+}
+
+// One CTA of 1024 threads: segments per slot, their exclusive prefix, the item
+// count, and both tickets reset for the pass.
+__global__ void __launch_bounds__(1024)
+k_solve_queue(const int* __restrict__ cnt, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups, SolveQueue q)
+{
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int base = 0; base < 2 * Kc; base += 1024) {
+        const int slot = base + (int)threadIdx.x;
+        int nseg = 0;
+        if (slot < 2 * Kc) {
+            const int env = slot / Kc, kk = slot - env * Kc;
+            const int E = cnt[env * g.K + k0 + kk];
+            if (E <= g.cap && E >= 2) {
+                const int Se = solve_seg_len(E, g.cap, S, Ss, H);
+                nseg = (E + Se - 1) / Se;
+            }
+        }
+        int incl = nseg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            const int v = wsum[lane];
+            int iv = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(kFull, iv, o);
+                if (lane >= o) iv += t;
+            }
+            wsum[lane] = iv - v;
+        }
+        __syncthreads();
+        const int c0 = carry;
+        if (slot < 2 * Kc) q.pref[slot] = c0 + wsum[wid] + incl - nseg;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c0 + wsum[wid] + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        q.pref[2 * Kc] = carry;
+        *q.total = carry * ngroups;
+        q.ticket[0] = 0;
+        q.ticket[1] = 0;
+    }
 }
 
 template <typename real, typename XT, bool XM, bool EPB, bool NAK>
@@ -563,7 +672,7 @@ __global__ void __launch_bounds__(kSolveThreads)
 k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
             real* __restrict__ dbuf, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
             unsigned* __restrict__ bnd, const XT* __restrict__ X, const int* __restrict__ knots,
-            const real* __restrict__ yend, Epochs ep)
+            const real* __restrict__ yend, Epochs ep, SolveQueue q)
 {
     // XM: knot values read from the working signal, y_i = X[x_i] (interior
     // knots) and yend (the clamped end knots of each record), instead of yv;
@@ -571,8 +680,10 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     // Rows of a record's end knots are the identity rows of the
     // factorisation (lm == 0): their right-hand side is 0.
     constexpr int B = kSolveBatch;
-    const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
-    if (!it.ok) return;  // uniform over the warp
+    SolveItem it;
+    bool first = true;
+    while (solve_next(it, first, 0, q, cnt, g, k0, Kc, S, Ss, H, ngroups)) {
+    if (!it.ok) continue;  // uniform over the warp
     const int lane = threadIdx.x & 31;
     const int C = g.C, E = it.E, i0 = it.i0, i1 = it.i1;
     const bool cok = it.c < C;
@@ -624,7 +735,7 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
         real fm = real(0), flm = real(0), fih = real(0);
         int fx = 0, ffl = 0, fe = 0;
         if (lane < nb) {
-            const Fac<real> fr = f[base + lane];
+            const Fac<real> fr = MEMD_CHECK(base + lane < g.cap) ? f[base + lane] : Fac<real>{};
             fm = fr.m;
             flm = fr.lm;
             fih = fr.ih;
@@ -669,7 +780,7 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
                 const real dcur = fmad_(-lm, dprev, mul_(m, r));
                 // rows before i0 only warm the recurrence up
                 if (FULL || i >= i0) {
-                    if (cok) o[(size_t)i * C] = dcur;
+                    if (cok && MEMD_CHECK(i >= 0 && i < g.cap)) o[(size_t)i * C] = dcur;
                     ymax = fmaxf(ymax, magf(yi));
                 }
                 slope_prev = slope;
@@ -686,13 +797,14 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
         if (i1 < E) ymax = fmaxf(ymax, magf(yi));  // right end of the last piece
         atomicMax(&bnd[it.c], __float_as_uint(ymax * 1.01f));
     }
+    }  // items
 }
 
 template <typename real, bool NAK>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, const real* __restrict__ dbuf,
             real* __restrict__ sv, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
-            unsigned* __restrict__ bnd, const int* __restrict__ knots)
+            unsigned* __restrict__ bnd, const int* __restrict__ knots, SolveQueue q)
 {
     // NAK (not-a-knot end conditions, g.nak), E >= 4: rows 0 and E-1 were solved as
     // identity rows; s_0 = s_1 + (h_0 / h_1)(s_1 - s_2) is applied at row 0,
@@ -700,8 +812,10 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     // warp that owns row E-3 (its window always reaches row E-1, and row E-2
     // does not depend on s_{E-1}), which also writes row E-1.
     constexpr int B = kSolveBatch;
-    const SolveItem it = solve_item(cnt, g, k0, Kc, S, Ss, H, ngroups);
-    if (!it.ok) return;
+    SolveItem it;
+    bool first = true;
+    while (solve_next(it, first, 1, q, cnt, g, k0, Kc, S, Ss, H, ngroups)) {
+    if (!it.ok) continue;  // uniform over the warp
     const int lane = threadIdx.x & 31;
     const int C = g.C, E = it.E, i0 = it.i0, i1 = it.i1;
     const bool cok = it.c < C;
@@ -722,13 +836,14 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
         const int nb = FULL ? B : min(B, top - i0 + 1);
         real fcp = real(0), fih = real(0);
         if (lane < nb) {
-            const Fac<real> fr = f[top - lane];
+            const Fac<real> fr = MEMD_CHECK(top - lane >= 0 && top - lane < g.cap) ? f[top - lane] : Fac<real>{};
             fcp = fr.cp;
             fih = fr.ih;
         }
         real db[B];
 #pragma unroll
-        for (int k = 0; k < B; ++k) db[k] = (FULL || k < nb) ? d[(size_t)(top - k) * C] : real(0);
+        for (int k = 0; k < B; ++k)
+            db[k] = ((FULL || k < nb) && MEMD_CHECK(top - k >= 0 && top - k < g.cap)) ? d[(size_t)(top - k) * C] : real(0);
 #pragma unroll
         for (int k = 0; k < B; ++k) {
             const real cp = shfl_idx_(fcp, k), ihr = shfl_idx_(fih, k);
@@ -740,7 +855,7 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
                         sol = add_(snext, div_(mul_(sub_(snext, snext2), real(kn[1] - kn[0])), real(kn[2] - kn[1])));
                 }
                 if (FULL || i < i1) {
-                    if (cok && !(NAK && nak && i == E - 1)) o[(size_t)i * C] = sol;
+                    if (cok && !(NAK && nak && i == E - 1) && MEMD_CHECK(i >= 0 && i < g.cap)) o[(size_t)i * C] = sol;
                     if (bnd && (FULL || i < E - 1)) {
                         // h^2 = 1 / ih^2 (9 / ih^2 when ih holds 3/h); the approximate
                         // division's error is inside the 1.01 margin applied at the end
@@ -767,6 +882,7 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
         else batch(std::false_type{}, top);
     }
     if (bnd && cok) atomicMax(&bnd[C + it.c], __float_as_uint(spart * 1.01f));
+    }  // items
 }
 
 // ---------------------------------------------------------------------------
@@ -1496,7 +1612,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
 #pragma unroll
                     for (int k = 0; k < KB; ++k) {
                         const unsigned long long qcur = qfix((sn[k] - sj) * r3[k], sh);
-                        atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
+                        if (MEMD_CHECK(xj - p0 >= 0 && xj - p0 < nl + 3)) atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
                         qprev = qcur;
                         xj = xn[k];
                         sj = sn[k];
@@ -1506,7 +1622,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
                     const int xn1 = kn[j0 + t0 + 1];
                     const dd sn1 = sv[rb + (size_t)(j0 + t0 + 1) * C];
                     const unsigned long long qcur = qfix((sn1 - sj) * rtab3[xn1 - xj], sh);
-                    atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
+                    if (MEMD_CHECK(xj - p0 >= 0 && xj - p0 < nl + 3)) atomicAdd(&kq[(xj - p0) * G + cc], qcur - qprev);
                     qprev = qcur;
                     xj = xn1;
                     sj = sn1;

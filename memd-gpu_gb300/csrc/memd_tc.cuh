@@ -1,54 +1,63 @@
 // memd_tc.cuh -- projection + extrema bitmasks on the tensor cores (mixed form).
 //
-// P[n][k] = sum_c X[n][c] dir[k][c] (reference: cublasSgemm,
-// memReducedEpochs_dev.cu:1182-1184, followed by the extrema flags of
-// find_extrema_shfl_max/min :77-141) as a 128-sample x N-direction tile per
-// CTA on the 5th-generation tensor cores:
+// The reference projects with cublasSgemm (memReducedEpochs_dev.cu:1182-1184)
+// and then flags strict local extrema of every projected direction
+// (find_extrema_shfl_max/min :77-141).  Here the tensor cores compute, per
+// tile of 128 samples and N <= 256 directions, the projected first differences
+//     D[n][k] = P[n][k] - P[n-1][k] = sum_c dir[k][c] (X[n][c] - X[n-1][c])
+// and sample n is a maximum (minimum) of direction k when D[n] > 0 > D[n+1]
+// (D[n] < 0 < D[n+1]): the same strict comparisons P[n] > P[n-1], P[n] >
+// P[n+1] as the reference, read from the signs of the differences.
 //
-//   k_split_tf32    the working signal's high words (double-float X[n][c].x)
-//                   and the directions' high words split into tf32 "big" and
-//                   "small" parts, x = big + small + r with |r| <= 2^-22 |x|,
+//   k_split_tf32    the first differences of the working signal (double-float
+//                   X[n][c], differenced in double-float, rounded to float)
+//                   and the directions' high words, each split into tf32 "big"
+//                   and "small" parts, v = big + small + r, |r| <= 2^-22 |v|,
 //                   stored [rows][Cp] (Cp = C rounded up to 32, zero padded)
 //   k_project_tc    TMA (cp.async.bulk.tensor, 128-byte swizzle) stages the
 //                   big / small tiles of 128 samples and N directions per
 //                   32-channel block; one thread issues the 3xTF32 products
 //                   big.big + big.small + small.big as tcgen05.mma kind::tf32
 //                   (M = 128, N <= 256, K = 8 per instruction) into a TMEM
-//                   accumulator; four warps read it back (tcgen05.ld, one
-//                   TMEM lane = one sample per thread) and form the extremum
-//                   tests with their neighbours by shuffle, the words of the
-//                   bitmask by ballot.
+//                   accumulator; four warps read it back (tcgen05.ld: one TMEM
+//                   lane = one sample per thread), take D[n+1] from the next
+//                   lane, warp or the tile's halo row, and form the bitmask
+//                   words by ballot.
 //
-// Certification (the extrema sets stay those of the FP64 projection, as in
-// k_project_mx).  With S = sum_c |dh_c| max|xh_c| over the tile (and its two
-// neighbour rows), the tensor-core value differs from the exact projection by
-// at most
-//   (4C + 8) 2^-22 S            products: the dropped small.small and
-//                               remainder terms (3.01 2^-22 |x||d| each) and
-//                               accumulation, counted as 2 ulp of the
-//                               largest partial sum per product and step
-//   + 2^-24 S + sum|dl| max|X|  the double-float low words of X and dir
-// (times 1.01).  A comparison whose tensor-core margin is within twice that
-// bound is redone with an FP32 fma dot product in channel order (bound
-// (C+2) 2^-24 S + sum|dl| max|X|, as k_project_mx), and one still within
-// twice that bound with double-float dot products (~2^-44).
+// Certification.  With S = sum_c |dh_c| max|dx_c| over the tile's rows and its
+// halo row (dx the rounded differences, dh / dl the direction's high / low
+// words), the tensor-core D differs from the exact difference of the
+// projections by at most
+//   (4C + 8) 2^-22 S       the dropped small.small and remainder terms
+//                          (3.01 2^-22 |dx||d| per product) and the
+//                          accumulation, counted as 2 ulp of the largest
+//                          partial sum per product and step
+//   + 2^-24 S              the rounding of the differences to float
+//   + sum_c |dl_c| max|dx_c|  the directions' low words
+// (times 1.01).  A sign within that bound of zero is decided again by a
+// double-float dot product of the double-float differences (~2^-44 relative),
+// so the extrema sets are those of the exact projection except at ties closer
+// than that.  Differencing first makes the bound scale with the signal's
+// sample-to-sample change rather than its size: smooth late-IMF signals, whose
+// neighbouring projections agree to many digits, stay decidable on the tensor
+// cores.
 //
 // Every wait on an mbarrier is bounded (iterations and clock); a wait that
 // runs out sets MEMD_FLAG_DEVICE_TIMEOUT in the run state, waits (bounded)
-// for the copies and products already issued, frees the TMEM columns and
+// for the copies or products already issued, frees the TMEM columns and
 // returns.
 #pragma once
 
 #include <cuda.h>
 
-#include "memd_kernels.cuh"  // kFull, df_dot, df_gt, sample_rule
+#include "memd_kernels.cuh"  // kFull, sample_rule
 #include "memd_ptx.cuh"
 
 namespace memd {
 
 constexpr int kTcRows = 128;        // samples per tile (MMA M)
 constexpr int kTcThreads = 128;     // four warps: one TMEM lane quarter each
-constexpr int kTcMaxN = 256;        // directions per tile (MMA N)
+constexpr int kTcMaxN = 256;        // directions per tile at most (MMA N)
 constexpr int kTcKB = 32;           // channels per K block (one 128-byte swizzled row of tf32)
 constexpr long long kTcWaitClocks = 1ll << 31;  // ~1 s at 2 GHz: the limit of every wait
 
@@ -77,20 +86,33 @@ __device__ __forceinline__ float tf32_rna(float x)
     return __uint_as_float(r);
 }
 
+// First difference of the double-float signal, X[n][c] - X[n-1][c], as a
+// double-float.
+__device__ __forceinline__ dd xdiff(float2 a, float2 b) { return dd(a.x, a.y) - dd(b.x, b.y); }
+
 // ---------------------------------------------------------------------------
-// Split into tf32 parts: big[r][c] = tf32(v), small[r][c] = tf32(v - big) of
-// v = src(r, c) for c < C, zero for C <= c < Cp.  src is the high word of a
-// double-float row-major [rows][C] array (stride 2 floats per element), or a
-// plain float array (stride 1).
+// Split into tf32 parts: big[r][c] = tf32(v), small[r][c] = tf32(v - big) for
+// c < C, zero for C <= c < Cp.
+//   diff = 1: v = float(X[r][c] - X[r-1][c]) of the double-float signal X
+//             ([rows][C] float2; v = 0 in row 0)
+//   diff = 0: v = src[r][c] of a float array ([rows][C])
 // ---------------------------------------------------------------------------
-__global__ void k_split_tf32(const float* __restrict__ src, int elem_stride, float* __restrict__ big,
+__global__ void k_split_tf32(const void* __restrict__ src, int diff, float* __restrict__ big,
                              float* __restrict__ small, int rows, int C, int Cp)
 {
     const size_t total = (size_t)rows * Cp;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const size_t r = i / Cp;
         const int c = (int)(i - r * Cp);
-        const float v = c < C ? src[(r * C + c) * elem_stride] : 0.f;
+        float v = 0.f;
+        if (c < C) {
+            if (diff) {
+                const float2* X = static_cast<const float2*>(src);
+                if (r > 0) v = xdiff(X[r * C + c], X[(r - 1) * C + c]).hi;
+            } else {
+                v = static_cast<const float*>(src)[r * C + c];
+            }
+        }
         const float b = tf32_rna(v);
         big[i] = b;
         small[i] = tf32_rna(__fsub_rn(v, b));
@@ -106,20 +128,39 @@ struct TcMaps {
 __host__ __device__ constexpr size_t tc_smem_bytes(int n)
 {
     return 1024 + 2 * (size_t)kTcRows * 128 + 2 * (size_t)n * 128  // operand tiles
-           + sizeof(float) * (8 * (size_t)kTcMaxN                  // edges [4][2][N]
-                              + 2 * (size_t)kTcMaxN                // halo rows [2][N]
-                              + 2 * (size_t)kTcMaxN                // thresholds [2][N]
+           + sizeof(float) * (4 * (size_t)kTcMaxN                  // first rows of the warps [4][N]
+                              + (size_t)kTcMaxN                    // halo row [N]
+                              + 2 * (size_t)kTcMaxN                // bound sums [2][N]
                               + 4 * 32 + 32)                       // channel maxima
            + 64;                                                   // barriers, TMEM address
 }
 
-__device__ __forceinline__ float proj_fma(const float2* __restrict__ xrow, const float* __restrict__ dh, int C)
+// sum_c dir[c] (X1[c] - X0[c]) in double-float (~2^-44 relative to
+// sum |dir| |X1 - X0|): double-float differences of the rows, two-product and
+// two-sum accumulation in channel order.
+__device__ __forceinline__ dd df_dot_diff(const float2* __restrict__ x1, const float2* __restrict__ x0,
+                                          const float* __restrict__ dh, const float* __restrict__ dl, int C)
 {
-    float acc = 0.f;
-    for (int c = 0; c < C; ++c) acc = __fmaf_rn(xrow[c].x, dh[c], acc);
-    return acc;
+    float hi = 0.f, lo = 0.f;
+    for (int c = 0; c < C; ++c) {
+        const dd v = xdiff(x1[c], x0[c]);
+        const float a = dh[c], al = dl[c];
+        const float p = __fmul_rn(a, v.hi);
+        float e = __fmaf_rn(a, v.hi, -p);
+        e = __fmaf_rn(a, v.lo, __fmaf_rn(al, v.hi, e));
+        const float s = __fadd_rn(hi, p);
+        const float bb = __fsub_rn(s, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+        lo = __fadd_rn(lo, __fadd_rn(err, e));
+        hi = s;
+    }
+    return dd_renorm(hi, lo);
 }
+__device__ __forceinline__ int dd_sign(dd v) { return v.hi > 0.f ? 1 : (v.hi < 0.f ? -1 : (v.lo > 0.f) - (v.lo < 0.f)); }
 
+// Grid: (ceil(L / 128), ceil(Kc / nt)); nt = directions per tile (a multiple
+// of 16 in [16, 256]; narrower tiles give more CTAs, each loading the same
+// signal tile).
 __global__ void __launch_bounds__(kTcThreads)
 k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, const float* __restrict__ dh_all,
              const float* __restrict__ dl_all, uint32_t* __restrict__ bits, Geom g, int k0, int Kc, int Cp, int nt,
@@ -130,13 +171,13 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
     // every 8 rows of 128 bytes)
     const uint32_t base = smem_u32(smem_raw);
     unsigned char* tiles = smem_raw + (((base + 1023u) & ~1023u) - base);
-    float* Ab = reinterpret_cast<float*>(tiles);             // [128][32]
-    float* As = Ab + kTcRows * kTcKB;                        // [128][32]
-    float* Bb = As + kTcRows * kTcKB;                        // [nt][32]
-    float* Bs = Bb + nt * kTcKB;                             // [nt][32]
-    float* edge = Bs + nt * kTcKB;                           // [4 warps][2][kTcMaxN]: lane 0 / lane 31 values
-    float* halo = edge + 8 * kTcMaxN;                        // [2][kTcMaxN]: rows n0 - 1, n0 + 128
-    float* thr = halo + 2 * kTcMaxN;                         // [2][kTcMaxN]: tensor-core / FP32 thresholds
+    float* Ab = reinterpret_cast<float*>(tiles);             // [128][32] big parts of the differences
+    float* As = Ab + kTcRows * kTcKB;                        // [128][32] small parts
+    float* Bb = As + kTcRows * kTcKB;                        // [nt][32] directions, big
+    float* Bs = Bb + nt * kTcKB;                             // [nt][32] directions, small
+    float* first = Bs + nt * kTcKB;                          // [4 warps][kTcMaxN]: D of each warp's lane 0
+    float* halo = first + 4 * kTcMaxN;                       // [kTcMaxN]: D at sample n0 + 128
+    float* thr = halo + kTcMaxN;                             // [2][kTcMaxN]: sum |dh| max|dx|, sum |dl| max|dx|
     float* cmx = thr + 2 * kTcMaxN;                          // [4][32] per-warp channel maxima
     float* mx = cmx + 4 * 32;                                // [32] channel maxima of the block
     uint64_t* bars = reinterpret_cast<uint64_t*>(mx + 32);   // [0] TMA, [1] MMA
@@ -145,10 +186,12 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int C = g.C;
     const int n0 = blockIdx.x * kTcRows;
-    const int kt0 = blockIdx.y * kTcMaxN;       // first direction of the tile within the chunk
+    const int kt0 = blockIdx.y * nt;            // first direction of the tile within the chunk
     const int nk = min(nt, Kc - kt0);           // valid directions of the tile
     const uint32_t ncols = nt <= 32 ? 32u : (nt <= 64 ? 64u : (nt <= 128 ? 128u : 256u));
     const int nkb = Cp / kTcKB;
+    const int nh = n0 + kTcRows;                // the halo row
+    const bool has_halo = nh < g.L;
 
     if (warp == 0) {
         tmem_alloc(s_taddr, ncols);
@@ -168,20 +211,31 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
     tc_fence_after();
     const uint32_t taddr = *s_taddr;
 
-    // halo rows n0 - 1 and n0 + 128 in FP32 (fma over the channels in order)
-    for (int i = tid; i < 2 * nk; i += kTcThreads) {
-        const int side = i / nk, kk = i - side * nk;
-        const int n = side ? n0 + kTcRows : n0 - 1;
-        float v = 0.f;
-        if (n >= 0 && n < g.L) v = proj_fma(X + (size_t)n * C, dh_all + (size_t)(k0 + kt0 + kk) * C, C);
-        halo[side * kTcMaxN + kk] = v;
-    }
-
     const uint32_t idesc = tc_idesc_tf32(nt);
     const uint32_t tx_bytes = (uint32_t)(2 * kTcRows * 128 + 2 * nt * 128);
+    if (tid == 0) {  // the first block's copies, before anything else
+        mbar_expect_tx(&bars[0], tx_bytes);
+        tma_load_2d(Ab, &maps.xb, &bars[0], 0, n0);
+        tma_load_2d(As, &maps.xs, &bars[0], 0, n0);
+        tma_load_2d(Bb, &maps.db, &bars[0], 0, k0 + kt0);
+        tma_load_2d(Bs, &maps.ds, &bars[0], 0, k0 + kt0);
+    }
+    // halo: D at sample n0 + 128 in FP32 from the rounded differences (the
+    // same numbers the tensor cores see), its error within the same bound
+    for (int kk = tid; kk < nk; kk += kTcThreads) {
+        float v = 0.f;
+        if (has_halo) {
+            const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
+            const float2* x1 = X + (size_t)nh * C;
+            const float2* x0 = x1 - C;
+            for (int c = 0; c < C; ++c) v = __fmaf_rn(dh[c], xdiff(x1[c], x0[c]).hi, v);
+        }
+        halo[kk] = v;
+    }
+
     int fail = 0, kb = 0;  // fail: 1 = a copy, 2 = the products did not complete in time
     for (; kb < nkb; ++kb) {
-        if (tid == 0) {
+        if (tid == 0 && kb > 0) {
             mbar_expect_tx(&bars[0], tx_bytes);
             tma_load_2d(Ab, &maps.xb, &bars[0], kb * kTcKB, n0);
             tma_load_2d(As, &maps.xs, &bars[0], kb * kTcKB, n0);
@@ -205,12 +259,13 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
             }
             mma_commit(&bars[1]);
         }
-        // channel maxima of this block over the tile's rows (the big parts;
-        // |x| <= |big| (1 + 2^-10)) while the products run: lane = channel,
-        // warp w = rows 32w .. 32w + 31; element (r, c) of the swizzled tile
-        // sits in 16-byte chunk (c / 4) ^ (r % 8) of row r
+        // channel maxima of |dx| over the tile's rows (the big parts;
+        // |big + small| <= |big| (1 + 2^-10)) while the products run: lane =
+        // channel, warp w = rows 32w .. 32w + 31; element (r, c) of the
+        // swizzled tile sits in 16-byte chunk (c / 4) ^ (r % 8) of row r
         {
             float m = 0.f;
+#pragma unroll 8
             for (int rr = 0; rr < 32; ++rr) {
                 const int r = warp * 32 + rr;
                 const int chunk = (lane >> 2) ^ (r & 7);
@@ -222,15 +277,11 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         if (warp == 0) {
             float m = fmaxf(fmaxf(cmx[lane], cmx[32 + lane]), fmaxf(cmx[64 + lane], cmx[96 + lane]));
             const int c = kb * kTcKB + lane;
-            // the halo rows' values
-            if (c < C) {
-                if (n0 - 1 >= 0) m = fmaxf(m, fabsf(X[(size_t)(n0 - 1) * C + c].x));
-                if (n0 + kTcRows < g.L) m = fmaxf(m, fabsf(X[(size_t)(n0 + kTcRows) * C + c].x));
-            }
-            mx[lane] = m * 1.0009765625f;  // |big + small| <= |big| (1 + 2^-10)
+            if (c < C && has_halo) m = fmaxf(m, fabsf(xdiff(X[(size_t)nh * C + c], X[(size_t)(nh - 1) * C + c]).hi));
+            mx[lane] = m * 1.0009765625f;
         }
         __syncthreads();
-        // partial bounds of this block: thr[k] += sum_c |dh| mx, thr[N + k] += sum_c |dl| mx
+        // this block's part of the bound sums
         for (int kk = tid; kk < nk; kk += kTcThreads) {
             const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
             const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
@@ -264,75 +315,57 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         }
         return;
     }
-    // thresholds: twice the error bounds, with the margin for their own rounding
+    // the bound on |D_tc - D| per direction, with the margin for its own rounding
     {
-        const float eps_tc = (float)(4 * C + 8) * 2.384185791e-7f + 5.9604645e-8f;  // (4C + 8) 2^-22 + 2^-24
-        const float eps_f = (float)(C + 2) * 5.9604645e-8f;                           // (C + 2) 2^-24
-        for (int kk = tid; kk < nk; kk += kTcThreads) {
-            const float sh = thr[kk], sl = thr[kTcMaxN + kk] * 1.0000002f;
-            thr[kk] = 2.02f * __fmaf_ru(eps_tc, sh, sl);
-            thr[kTcMaxN + kk] = 2.02f * __fmaf_ru(eps_f, sh, sl);
-        }
+        const float eps = (float)(4 * C + 8) * 2.384185791e-7f + 5.9604645e-8f;  // (4C + 8) 2^-22 + 2^-24
+        for (int kk = tid; kk < nk; kk += kTcThreads)
+            thr[kk] = 1.01f * __fmaf_ru(eps, thr[kk], thr[kTcMaxN + kk] * 1.0000002f);
     }
-    // pass 1: every warp publishes its first and last rows for the neighbours
+    // pass 1: every warp publishes its lane 0 (its first sample) for the warp before
     const uint32_t tl = taddr + ((uint32_t)(warp * 32) << 16);
     for (int j0 = 0; j0 < nt; j0 += 32) {
         float v[32];
-        __syncwarp();
+        (void)MEMD_CHECK(j0 + 32 <= (int)ncols && j0 + 32 <= kTcMaxN);
+        __syncwarp();  // tcgen05.ld is warp-collective
         tmem_ld32(tl + (uint32_t)j0, v);
-        if (lane == 0 || lane == 31) {
-            float* e = edge + (warp * 2 + (lane == 31)) * kTcMaxN + j0;
+        if (lane == 0) {
+            float* e = first + warp * kTcMaxN + j0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) e[j] = v[j];
         }
     }
     __syncthreads();
-    // pass 2: extremum tests, ballots, one bitmask word per lane and direction
-    const int r = warp * 32 + lane;
-    const int n = n0 + r;
+    // pass 2: signs of D[n] and D[n+1], ballots, one bitmask word per lane and direction
+    const int n = n0 + warp * 32 + lane;
     bool inrange, endpt, interior;
     sample_rule(g, ep, n, inrange, endpt, interior);
     const int w = (n0 >> 5) + warp;
-    int refined = 0, rechecked = 0;
+    int refined = 0;
     for (int j0 = 0; j0 < nt; j0 += 32) {
         float v[32];
-        __syncwarp();  // tcgen05.ld is warp-collective
+        __syncwarp();
         tmem_ld32(tl + (uint32_t)j0, v);
         uint32_t my_max = 0u, my_min = 0u;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const int kk = j0 + j;
-            const float p = v[j];
-            float pl = __shfl_up_sync(kFull, p, 1);
-            float pn = __shfl_down_sync(kFull, p, 1);
-            if (lane == 0) pl = warp == 0 ? halo[kk] : edge[((warp - 1) * 2 + 1) * kTcMaxN + kk];
-            if (lane == 31) pn = warp == 3 ? halo[kTcMaxN + kk] : edge[((warp + 1) * 2) * kTcMaxN + kk];
-            bool mxf = p > pl && p > pn;
-            bool mnf = p < pl && p < pn;
-            const bool kok = kk < nk;
-            if (interior && kok) {
-                const float t1 = thr[kk];
-                if (fabsf(__fsub_rn(p, pl)) <= t1 || fabsf(__fsub_rn(p, pn)) <= t1) {
-                    // within the tensor-core bound: FP32 dot products in channel order
+            const float d0 = v[j];  // D[n]
+            float d1 = __shfl_down_sync(kFull, d0, 1);
+            if (lane == 31) d1 = warp == 3 ? halo[kk] : first[(warp + 1) * kTcMaxN + kk];
+            bool mxf = d0 > 0.f && d1 < 0.f;
+            bool mnf = d0 < 0.f && d1 > 0.f;
+            if (interior && kk < nk) {
+                const float t = thr[kk];
+                if (fabsf(d0) <= t || fabsf(d1) <= t) {
+                    // a sign within the bound: double-float differences
                     const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
-                    const float a = proj_fma(X + (size_t)(n - 1) * C, dh, C);
-                    const float b = proj_fma(X + (size_t)n * C, dh, C);
-                    const float c2 = proj_fma(X + (size_t)(n + 1) * C, dh, C);
-                    const float t2 = thr[kTcMaxN + kk];
-                    ++rechecked;
-                    if (fabsf(__fsub_rn(b, a)) <= t2 || fabsf(__fsub_rn(b, c2)) <= t2) {
-                        // still within the FP32 bound: double-float
-                        const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
-                        const float2 da = df_dot(X + (size_t)(n - 1) * C, dh, dl, C);
-                        const float2 db = df_dot(X + (size_t)n * C, dh, dl, C);
-                        const float2 dc = df_dot(X + (size_t)(n + 1) * C, dh, dl, C);
-                        mxf = df_gt(db, da) && df_gt(db, dc);
-                        mnf = df_gt(da, db) && df_gt(dc, db);
-                        ++refined;
-                    } else {
-                        mxf = b > a && b > c2;
-                        mnf = b < a && b < c2;
-                    }
+                    const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
+                    const float2* xn = X + (size_t)n * C;
+                    const int s0 = dd_sign(df_dot_diff(xn, xn - C, dh, dl, C));
+                    const int s1 = dd_sign(df_dot_diff(xn + C, xn, dh, dl, C));
+                    mxf = s0 > 0 && s1 < 0;
+                    mnf = s0 < 0 && s1 > 0;
+                    ++refined;
                 }
             }
             const uint32_t wmax = __ballot_sync(kFull, inrange && (endpt || (interior && mxf)));
@@ -343,15 +376,13 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
             }
         }
         const int kk = j0 + lane;
-        if (kk < nk && w < g.W) {
+        if (kk < nk && w < g.W && MEMD_CHECK(kt0 + kk < Kc)) {
             bits[(size_t)(kt0 + kk) * g.W + w] = my_max;
             bits[(size_t)(Kc + kt0 + kk) * g.W + w] = my_min;
         }
     }
     refined = warp_sum(refined);
-    rechecked = warp_sum(rechecked);
     if (lane == 0 && refined) atomicAdd(&st->pad[3], refined);
-    if (lane == 0 && rechecked) atomicAdd(&st->rechecked, rechecked);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {

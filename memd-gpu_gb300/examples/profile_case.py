@@ -7,7 +7,8 @@ eeg32:   32 channels x 30,504 samples (EEG-shaped, seed 0), 128 directions, 9 sl
 batched: N epochs of 32 channels, lengths uniform in [1024, 8192] (seed 1000), 64 directions,
          8 slots x 10 sifts, one batched call.
 Each run launches the decomposition graph once; the kernel order within a run is
-project, compact, factor, solve (forward, backward), mean, per sift.
+project (mixed form: tf32 split, then the tensor-core projection), compact, factor,
+solve (forward, backward), mean, per sift.
 """
 import argparse
 import os
@@ -28,16 +29,19 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "f64", "f32"])
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--runs", type=int, default=1)
+    ap.add_argument("--projection", default="auto", choices=["auto", "cuda-cores"],
+                    help="mixed form: tensor-core (auto) or CUDA-core projection")
     a = ap.parse_args()
     if a.runs < 1:
         ap.error("--runs must be at least 1")
     prec = {"mixed": mg.PREC_MIXED, "f64": mg.PREC_F64, "f32": mg.PREC_F32}[a.precision]
+    proj = mg.PROJ_AUTO if a.projection == "auto" else mg.PROJ_CUDA_CORES
     tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
     if a.case == "eeg32":
         C, L, K = 32, 30504, 128
         y = torch.as_tensor(mg.synth_eeg(C, L, 256.0, seed=0).astype(np.float32), dtype=tdt, device="cuda")
         d = mg.directions(C, K, dtype="f32").to(tdt)
-        plan = mg.Plan(C, L, K, 9, 10, precision=prec)
+        plan = mg.Plan(C, L, K, 9, 10, precision=prec, projection=proj)
         out = torch.empty((9, C, L), dtype=tdt, device="cuda")
         for _ in range(a.runs):
             st = plan.run(y, d, out)
@@ -49,11 +53,12 @@ def main():
         offs = np.concatenate([[0], np.cumsum(C * lengths)[:-1]]).astype(np.int64)
         y = torch.as_tensor(np.concatenate([r.ravel() for r in recs]), dtype=tdt, device="cuda")
         d = mg.directions(C, K, dtype="f32").to(tdt)
-        plan = mg.Plan(C, 8192, K, NI, IT, precision=prec, max_epochs=E)
+        plan = mg.Plan(C, 8192, K, NI, IT, precision=prec, max_epochs=E, projection=proj)
         out = torch.empty(NI * y.numel(), dtype=tdt, device="cuda")
         for _ in range(a.runs):
             st = plan.run_batched(y, lengths, offs, d, out)
-    print(f"{a.case} {a.precision}: {st.elapsed_ms:.3f} ms, {st.launches} launches, flags {st.flags}")
+    print(f"{a.case} {a.precision}: {st.elapsed_ms:.3f} ms, {st.launches} launches, flags {st.flags}, "
+          f"tests re-decided in double-float {st.refined}")
     plan.close()
 
 

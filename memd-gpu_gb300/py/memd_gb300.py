@@ -14,6 +14,9 @@ import numpy as np
 
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "lib", "libmemd_gb300.so")
+# the bounds-checked build of the same library (index checks report
+# FLAG_CHECK_FAILED instead of touching memory out of bounds; for tests)
+LIB_CHECKED_PATH = os.path.join(PKG, "lib", "libmemd_gb300_checked.so")
 
 MEMD_OK = 0
 MEMD_ERR_INVALID = 1
@@ -30,13 +33,15 @@ BOUNDARY_REFERENCE, BOUNDARY_MIRROR = 0, 1
 FLAG_NO_QUALIFIED_DIRECTION = 1
 FLAG_KNOT_OVERFLOW = 2
 FLAG_DEVICE_TIMEOUT = 4
+FLAG_CHECK_FAILED = 8
 PROJ_AUTO, PROJ_CUDA_CORES = 0, 1
 
 TRACE_DTYPE = np.dtype([("count", "<i4"), ("flags", "<i4"), ("hash", "<u8")])
 
 # every symbol include/memd_gb300.h and include/memd_synth.h declare
 EXPORTS = [
-    "memd_default_config", "memd_plan_create", "memd_plan_destroy", "memd_plan_workspace_bytes",
+    "memd_default_config", "memd_plan_create", "memd_plan_create_tuned", "memd_plan_get_tuning",
+    "memd_plan_destroy", "memd_plan_workspace_bytes",
     "memd_plan_set_trace", "memd_run_f64", "memd_run_f32", "memd_run_batched_f64",
     "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_profile_batched_f64",
     "memd_profile_batched_f32", "memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64", "memd_diag_fma_rate", "memd_diag_wait_timeout", "memd_last_error",
@@ -75,6 +80,31 @@ class Config(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    """Launch shapes of a plan (memd_tuning); 0 = the default."""
+    _fields_ = [
+        ("solve_segment", ctypes.c_int32),
+        ("solve_min_segment", ctypes.c_int32),
+        ("factor_segment", ctypes.c_int32),
+        ("solve_queue", ctypes.c_int32),
+        ("mean_ctas", ctypes.c_int32),
+        ("proj_tile_n", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 10),
+    ]
+    KEYS = ("solve_segment", "solve_min_segment", "factor_segment", "solve_queue", "mean_ctas", "proj_tile_n")
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k in self.KEYS}
+
+    @classmethod
+    def from_dict(cls, d):
+        t = cls()
+        for k, v in (d or {}).items():
+            if k in cls.KEYS:
+                setattr(t, k, int(v))
+        return t
+
+
 class Stats(ctypes.Structure):
     _fields_ = [
         ("n_imfs", ctypes.c_int32),
@@ -83,7 +113,7 @@ class Stats(ctypes.Structure):
         ("launches", ctypes.c_int64),
         ("sifts", ctypes.c_int32 * 64),
         ("refined", ctypes.c_int32),
-        ("rechecked", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 
@@ -98,20 +128,37 @@ class Profile(ctypes.Structure):
 
 
 _lib = None
+_lib_checked = None
 
 
 def lib():
     global _lib
-    if _lib is not None:
-        return _lib
-    if not os.path.exists(LIB_PATH):
-        raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() (nvcc, sm_103a)")
-    L = ctypes.CDLL(LIB_PATH)
+    if _lib is None:
+        _lib = _load(LIB_PATH)
+    return _lib
+
+
+def checked_lib():
+    """The bounds-checked build, bound like lib() (its own plans and state)."""
+    global _lib_checked
+    if _lib_checked is None:
+        _lib_checked = _load(LIB_CHECKED_PATH)
+    return _lib_checked
+
+
+def _load(path):
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run __graft_entry__.build() (nvcc, sm_103a)")
+    L = ctypes.CDLL(path)
     vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
     L.memd_default_config.argtypes = [ctypes.POINTER(Config)]
     L.memd_default_config.restype = None
     L.memd_plan_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(vp)]
     L.memd_plan_create.restype = ctypes.c_int
+    L.memd_plan_create_tuned.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Tuning), ctypes.POINTER(vp)]
+    L.memd_plan_create_tuned.restype = ctypes.c_int
+    L.memd_plan_get_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    L.memd_plan_get_tuning.restype = ctypes.c_int
     L.memd_plan_destroy.argtypes = [vp]
     L.memd_plan_destroy.restype = ctypes.c_int
     L.memd_plan_workspace_bytes.argtypes = [vp]
@@ -156,13 +203,12 @@ def lib():
     L.memd_bin_count.restype = i64
     L.memd_read_bin.argtypes = [ctypes.c_char_p, vp, i64, i32]
     L.memd_read_bin.restype = ctypes.c_int
-    _lib = L
     return L
 
 
-def _check(status: int):
+def _check(status: int, L=None):
     if status != MEMD_OK:
-        raise MemdError(status, lib().memd_last_error().decode())
+        raise MemdError(status, (L or lib()).memd_last_error().decode())
 
 
 def last_error() -> str:
@@ -198,26 +244,45 @@ class Plan:
     """Owns a memd_plan: all device buffers of one decomposition shape."""
 
     def __init__(self, channels: int, length: int, directions: int, num_imfs: int = 9,
-                 max_iter: int = 10, precision: int = PREC_F64, **kw):
+                 max_iter: int = 10, precision: int = PREC_F64, tuning=None, library=None, **kw):
+        """tuning: None (defaults), a dict / Tuning of launch shapes, or "auto"
+        (the autotuner's stored choice for this shape, if there is one).
+        library: the bound library (lib() by default; checked_lib() for the
+        bounds-checked build)."""
+        self._L = library or lib()
+        self._chk = lambda status: _check(status, self._L)
         self.cfg = default_config(channels=channels, length=length, directions=directions,
                                   num_imfs=num_imfs, max_iter=max_iter, precision=precision, **kw)
+        if isinstance(tuning, str):
+            if tuning != "auto":
+                raise ValueError("tuning must be None, a dict, a Tuning or 'auto'")
+            import memd_autotune
+
+            tuning = memd_autotune.lookup(self.cfg)
+        t = tuning if isinstance(tuning, Tuning) else Tuning.from_dict(tuning)
         h = ctypes.c_void_p()
-        _check(lib().memd_plan_create(ctypes.byref(self.cfg), ctypes.byref(h)))
+        self._chk(self._L.memd_plan_create_tuned(ctypes.byref(self.cfg), ctypes.byref(t), ctypes.byref(h)))
         self.handle = h
         self._trace = None
 
+    def tuning(self) -> dict:
+        """The launch shapes the plan uses (defaults filled in)."""
+        t = Tuning()
+        self._chk(self._L.memd_plan_get_tuning(self.handle, ctypes.byref(t)))
+        return t.as_dict()
+
     @property
     def workspace_bytes(self) -> int:
-        return int(lib().memd_plan_workspace_bytes(self.handle))
+        return int(self._L.memd_plan_workspace_bytes(self.handle))
 
     def set_trace(self, enable: bool = True):
         if enable:
             n = self.cfg.num_imfs * (self.cfg.max_iter + 1) * self.cfg.directions * 2
             self._trace = np.zeros(n, dtype=TRACE_DTYPE)
-            _check(lib().memd_plan_set_trace(self.handle, self._trace.ctypes.data_as(ctypes.c_void_p)))
+            self._chk(self._L.memd_plan_set_trace(self.handle, self._trace.ctypes.data_as(ctypes.c_void_p)))
         else:
             self._trace = None
-            _check(lib().memd_plan_set_trace(self.handle, None))
+            self._chk(self._L.memd_plan_set_trace(self.handle, None))
 
     def trace(self):
         if self._trace is None:
@@ -227,8 +292,8 @@ class Plan:
     def run(self, y, dirs, imfs, x=None, stream=None, stats: bool = True):
         """y: (C, L) device tensor, dirs: (K, C), imfs: (num_imfs, C, L); same dtype."""
         st = Stats()
-        fn = lib().memd_run_f64 if self.cfg.precision == PREC_F64 else lib().memd_run_f32
-        _check(fn(self.handle, _dptr(x), _dptr(y), _dptr(dirs), _dptr(imfs), _stream_ptr(stream),
+        fn = self._L.memd_run_f64 if self.cfg.precision == PREC_F64 else self._L.memd_run_f32
+        self._chk(fn(self.handle, _dptr(x), _dptr(y), _dptr(dirs), _dptr(imfs), _stream_ptr(stream),
                   ctypes.byref(st) if stats else None))
         return st if stats else None
 
@@ -240,8 +305,8 @@ class Plan:
         la = (ctypes.c_int64 * n)(*[int(v) for v in lengths])
         oa = (ctypes.c_int64 * n)(*[int(v) for v in offsets])
         st = Stats()
-        fn = lib().memd_run_batched_f64 if self.cfg.precision == PREC_F64 else lib().memd_run_batched_f32
-        _check(fn(self.handle, n, ctypes.cast(la, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p), _dptr(y),
+        fn = self._L.memd_run_batched_f64 if self.cfg.precision == PREC_F64 else self._L.memd_run_batched_f32
+        self._chk(fn(self.handle, n, ctypes.cast(la, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p), _dptr(y),
                   _dptr(dirs), _dptr(imfs), _stream_ptr(stream),
                   ctypes.byref(st) if stats else None))
         return st if stats else None
@@ -252,21 +317,21 @@ class Plan:
         la = (ctypes.c_int64 * n)(*[int(v) for v in lengths])
         oa = (ctypes.c_int64 * n)(*[int(v) for v in offsets])
         pr = Profile()
-        fn = lib().memd_profile_batched_f64 if self.cfg.precision == PREC_F64 else lib().memd_profile_batched_f32
-        _check(fn(self.handle, n, ctypes.cast(la, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p), _dptr(y),
+        fn = self._L.memd_profile_batched_f64 if self.cfg.precision == PREC_F64 else self._L.memd_profile_batched_f32
+        self._chk(fn(self.handle, n, ctypes.cast(la, ctypes.c_void_p), ctypes.cast(oa, ctypes.c_void_p), _dptr(y),
                   _dptr(dirs), _dptr(imfs), _stream_ptr(stream), ctypes.byref(pr)))
         return pr
 
     def profile(self, y, dirs, imfs, stream=None) -> Profile:
         """Eager run with every kernel timed by CUDA events (per-stage ms)."""
         pr = Profile()
-        fn = lib().memd_profile_f64 if self.cfg.precision == PREC_F64 else lib().memd_profile_f32
-        _check(fn(self.handle, _dptr(y), _dptr(dirs), _dptr(imfs), _stream_ptr(stream), ctypes.byref(pr)))
+        fn = self._L.memd_profile_f64 if self.cfg.precision == PREC_F64 else self._L.memd_profile_f32
+        self._chk(fn(self.handle, _dptr(y), _dptr(dirs), _dptr(imfs), _stream_ptr(stream), ctypes.byref(pr)))
         return pr
 
     def close(self):
         if getattr(self, "handle", None):
-            lib().memd_plan_destroy(self.handle)
+            self._L.memd_plan_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -242,13 +242,25 @@ def test_fp32_path_runs_fast_eval_and_reconstructs():
     assert np.abs(imfs.astype(np.float64).sum(axis=0) - y32).max() < 1e-3 * np.abs(y32).max()
 
 
-def test_mixed_stop_mode_runs():
-    y = mg.synth_tones(8, 2000, 1000.0, seed=1)
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mixed_stop_mode_matches_fp64_sift_counts(seed):
+    """Stop mode on the 8-channel tone record (64 directions, thresholds
+    0.075 / 0.75 / 0.075, up to 10 IMFs): the mixed form makes the FP64 path's
+    decisions -- the same number of IMFs, the same sift count for every IMF,
+    the same extrema sets at every pass -- and its IMFs are within 1e-6."""
+    import memd_signals
+
+    y = memd_signals.tones(8, 2000, 1000.0, seed=seed)
     d = oracle.directions(8, 64)
     y32, d32, y64, d64 = _as_f32_inputs(y, d)
-    a, sa, _ = run_gpu(y64, d64, 10, 50, stop_mode=mg.STOP_CRITERION)
-    b, sb, _ = run_gpu(y32, d32, 10, 50, precision=mg.PREC_MIXED, stop_mode=mg.STOP_CRITERION)
-    assert sb.n_imfs >= 1
+    a, sa, ta = run_gpu(y64, d64, 11, 200, trace=True, stop_mode=mg.STOP_CRITERION)
+    b, sb, tb = run_gpu(y32, d32, 11, 200, precision=mg.PREC_MIXED, trace=True, stop_mode=mg.STOP_CRITERION)
+    assert sb.n_imfs == sa.n_imfs >= 1
+    assert list(sb.sifts[: sb.n_imfs]) == list(sa.sifts[: sa.n_imfs])
+    assert np.array_equal(ta["count"], tb["count"]) and np.array_equal(ta["hash"], tb["hash"])
+    for i in range(11):
+        if np.linalg.norm(a[i]) > 0:
+            assert rel_l2(b[i], a[i]) < 1e-6, i
     assert np.abs(b.astype(np.float64).sum(axis=0) - y32).max() < 1e-4 * np.abs(y32).max()
 
 

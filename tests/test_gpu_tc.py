@@ -1,5 +1,6 @@
-"""The tensor-core projection of the mixed form (k_project_tc: TMA-staged
-tf32 tiles, 3xTF32 tcgen05.mma into TMEM, certified extremum tests) against
+"""The tensor-core projection of the mixed form (k_project_tc: TMA-staged tf32
+tiles of the signal's first differences, 3xTF32 tcgen05.mma into TMEM,
+certified signs of the projected differences) against
 the CUDA-core projection (k_project_mx) and the FP64 path: identical extrema
 index sets at every sift, so identical decompositions.
 
@@ -43,7 +44,6 @@ def test_tensor_core_projection_equals_cuda_core_and_fp64(C, L, K, chunk):
     assert np.array_equal(ta["count"], tb["count"]) and np.array_equal(ta["hash"], tb["hash"])
     assert np.array_equal(ta["count"], tc["count"]) and np.array_equal(ta["hash"], tc["hash"])
     assert np.array_equal(a, b)
-    assert sa.rechecked >= sa.refined
 
 
 def test_tensor_core_projection_in_batched_runs():

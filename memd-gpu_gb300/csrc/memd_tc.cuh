@@ -131,32 +131,38 @@ __host__ __device__ constexpr size_t tc_smem_bytes(int n)
            + sizeof(float) * (4 * (size_t)kTcMaxN                  // first rows of the warps [4][N]
                               + (size_t)kTcMaxN                    // halo row [N]
                               + 2 * (size_t)kTcMaxN                // bound sums [2][N]
-                              + 4 * 32 + 32)                       // channel maxima
+                              + 4 * 32 + 32                        // channel maxima
+                              + 2 * (size_t)n * 33                 // direction words of a block [2][N][33]
+                              + 32)                                // halo-row differences of a block
            + 64;                                                   // barriers, TMEM address
 }
 
-// sum_c dir[c] (X1[c] - X0[c]) in double-float (~2^-44 relative to
-// sum |dir| |X1 - X0|): double-float differences of the rows, two-product and
-// two-sum accumulation in channel order.
-__device__ __forceinline__ dd df_dot_diff(const float2* __restrict__ x1, const float2* __restrict__ x0,
-                                          const float* __restrict__ dh, const float* __restrict__ dl, int C)
+__device__ __forceinline__ int dd_sign(dd v) { return v.hi > 0.f ? 1 : (v.hi < 0.f ? -1 : (v.lo > 0.f) - (v.lo < 0.f)); }
+
+// The sign of sum_c dir[c] (X1[c] - X0[c]) in double-float, computed by the
+// whole warp: lane l takes channels l, l + 32, ... (one coalesced row load
+// per operand), the lanes' double-float partial sums meet in a butterfly of
+// shuffles; every lane returns lane 0's sign.  Each term is the exact
+// two-product of the direction's high word with the double-float difference
+// plus the low word's product, so the sum carries ~2^-44 relative to
+// sum |dir| |X1 - X0|.
+__device__ __noinline__ int warp_df_diff_sign(const float2* __restrict__ x1, const float2* __restrict__ x0,
+                                                 const float* __restrict__ dh, const float* __restrict__ dl, int C,
+                                                 int lane)
 {
-    float hi = 0.f, lo = 0.f;
-    for (int c = 0; c < C; ++c) {
+    dd acc(0.f, 0.f);
+    for (int c = lane; c < C; c += 32) {
         const dd v = xdiff(x1[c], x0[c]);
         const float a = dh[c], al = dl[c];
         const float p = __fmul_rn(a, v.hi);
         float e = __fmaf_rn(a, v.hi, -p);
         e = __fmaf_rn(a, v.lo, __fmaf_rn(al, v.hi, e));
-        const float s = __fadd_rn(hi, p);
-        const float bb = __fsub_rn(s, hi);
-        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-        lo = __fadd_rn(lo, __fadd_rn(err, e));
-        hi = s;
+        acc = acc + dd_renorm(p, e);
     }
-    return dd_renorm(hi, lo);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc = acc + shfl_xor_(acc, o);
+    return __shfl_sync(kFull, dd_sign(acc), 0);
 }
-__device__ __forceinline__ int dd_sign(dd v) { return v.hi > 0.f ? 1 : (v.hi < 0.f ? -1 : (v.lo > 0.f) - (v.lo < 0.f)); }
 
 // Grid: (ceil(L / 128), ceil(Kc / nt)); nt = directions per tile (a multiple
 // of 16 in [16, 256]; narrower tiles give more CTAs, each loading the same
@@ -180,7 +186,10 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
     float* thr = halo + kTcMaxN;                             // [2][kTcMaxN]: sum |dh| max|dx|, sum |dl| max|dx|
     float* cmx = thr + 2 * kTcMaxN;                          // [4][32] per-warp channel maxima
     float* mx = cmx + 4 * 32;                                // [32] channel maxima of the block
-    uint64_t* bars = reinterpret_cast<uint64_t*>(mx + 32);   // [0] TMA, [1] MMA
+    float* dhs = mx + 32;                                    // [nt][33] direction high words of the block
+    float* dls = dhs + nt * 33;                              // [nt][33] low words
+    float* xd = dls + nt * 33;                               // [32] halo-row differences of the block
+    uint64_t* bars = reinterpret_cast<uint64_t*>(xd + 32);   // [0] TMA, [1] MMA
     uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bars + 2);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -221,17 +230,9 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         tma_load_2d(Bs, &maps.ds, &bars[0], 0, k0 + kt0);
     }
     // halo: D at sample n0 + 128 in FP32 from the rounded differences (the
-    // same numbers the tensor cores see), its error within the same bound
-    for (int kk = tid; kk < nk; kk += kTcThreads) {
-        float v = 0.f;
-        if (has_halo) {
-            const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
-            const float2* x1 = X + (size_t)nh * C;
-            const float2* x0 = x1 - C;
-            for (int c = 0; c < C; ++c) v = __fmaf_rn(dh[c], xdiff(x1[c], x0[c]).hi, v);
-        }
-        halo[kk] = v;
-    }
+    // same numbers the tensor cores see), its error within the same bound;
+    // summed over the channel blocks below
+    for (int kk = tid; kk < nt; kk += kTcThreads) halo[kk] = 0.f;
 
     int fail = 0, kb = 0;  // fail: 1 = a copy, 2 = the products did not complete in time
     for (; kb < nkb; ++kb) {
@@ -241,6 +242,18 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
             tma_load_2d(As, &maps.xs, &bars[0], kb * kTcKB, n0);
             tma_load_2d(Bb, &maps.db, &bars[0], kb * kTcKB, k0 + kt0);
             tma_load_2d(Bs, &maps.ds, &bars[0], kb * kTcKB, k0 + kt0);
+        }
+        // this block's direction words and halo-row differences into shared
+        // memory (coalesced, while the copies land)
+        for (int i = tid; i < nt * kTcKB; i += kTcThreads) {
+            const int kk = i >> 5, c = kb * kTcKB + (i & 31);
+            const bool ok = kk < nk && c < C;
+            dhs[kk * 33 + (i & 31)] = ok ? dh_all[(size_t)(k0 + kt0 + kk) * C + c] : 0.f;
+            dls[kk * 33 + (i & 31)] = ok ? dl_all[(size_t)(k0 + kt0 + kk) * C + c] : 0.f;
+        }
+        if (tid < 32) {
+            const int c = kb * kTcKB + tid;
+            xd[tid] = (has_halo && c < C) ? xdiff(X[(size_t)nh * C + c], X[(size_t)(nh - 1) * C + c]).hi : 0.f;
         }
         const bool got = mbar_wait_bounded(&bars[0], (uint32_t)(kb & 1), kTcWaitClocks);
         if (__syncthreads_or(!got)) {  // the same decision in every thread
@@ -275,22 +288,22 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         }
         __syncthreads();
         if (warp == 0) {
-            float m = fmaxf(fmaxf(cmx[lane], cmx[32 + lane]), fmaxf(cmx[64 + lane], cmx[96 + lane]));
-            const int c = kb * kTcKB + lane;
-            if (c < C && has_halo) m = fmaxf(m, fabsf(xdiff(X[(size_t)nh * C + c], X[(size_t)(nh - 1) * C + c]).hi));
-            mx[lane] = m * 1.0009765625f;
+            const float m = fmaxf(fmaxf(cmx[lane], cmx[32 + lane]), fmaxf(cmx[64 + lane], cmx[96 + lane]));
+            mx[lane] = fmaxf(m, fabsf(xd[lane])) * 1.0009765625f;
         }
         __syncthreads();
-        // this block's part of the bound sums
+        // this block's part of the halo row and of the bound sums
         for (int kk = tid; kk < nk; kk += kTcThreads) {
-            const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
-            const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
-            float sh = thr[kk], sl = thr[kTcMaxN + kk];
-            const int c1 = min(C, (kb + 1) * kTcKB);
-            for (int c = kb * kTcKB; c < c1; ++c) {
-                sh = __fmaf_ru(fabsf(dh[c]), mx[c - kb * kTcKB], sh);
-                sl = __fmaf_ru(fabsf(dl[c]), mx[c - kb * kTcKB], sl);
+            const float* dh = dhs + kk * 33;
+            const float* dl = dls + kk * 33;
+            float h = halo[kk], sh = thr[kk], sl = thr[kTcMaxN + kk];
+            const int nc = min(kTcKB, C - kb * kTcKB);
+            for (int c = 0; c < nc; ++c) {
+                h = __fmaf_rn(dh[c], xd[c], h);
+                sh = __fmaf_ru(fabsf(dh[c]), mx[c], sh);
+                sl = __fmaf_ru(fabsf(dl[c]), mx[c], sl);
             }
+            halo[kk] = h;
             thr[kk] = sh;
             thr[kTcMaxN + kk] = sl;
         }
@@ -345,31 +358,51 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         float v[32];
         __syncwarp();
         tmem_ld32(tl + (uint32_t)j0, v);
-        uint32_t my_max = 0u, my_min = 0u;
+        // bit j of each mask: direction j0 + j at this lane's sample
+        uint32_t mxm = 0u, mnm = 0u, nearm = 0u;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const int kk = j0 + j;
             const float d0 = v[j];  // D[n]
             float d1 = __shfl_down_sync(kFull, d0, 1);
             if (lane == 31) d1 = warp == 3 ? halo[kk] : first[(warp + 1) * kTcMaxN + kk];
-            bool mxf = d0 > 0.f && d1 < 0.f;
-            bool mnf = d0 < 0.f && d1 > 0.f;
+            if (d0 > 0.f && d1 < 0.f) mxm |= 1u << j;
+            if (d0 < 0.f && d1 > 0.f) mnm |= 1u << j;
             if (interior && kk < nk) {
                 const float t = thr[kk];
-                if (fabsf(d0) <= t || fabsf(d1) <= t) {
-                    // a sign within the bound: double-float differences
-                    const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
-                    const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
-                    const float2* xn = X + (size_t)n * C;
-                    const int s0 = dd_sign(df_dot_diff(xn, xn - C, dh, dl, C));
-                    const int s1 = dd_sign(df_dot_diff(xn + C, xn, dh, dl, C));
-                    mxf = s0 > 0 && s1 < 0;
-                    mnf = s0 < 0 && s1 > 0;
-                    ++refined;
+                if (fabsf(d0) <= t || fabsf(d1) <= t) nearm |= 1u << j;
+            }
+        }
+        refined += __popc(nearm);
+        // signs within the bound: decided again in double-float, one
+        // (direction, lane) at a time by the whole warp (lanes over channels)
+        uint32_t anyj = __reduce_or_sync(kFull, nearm);
+        while (anyj) {
+            const int j = __ffs(anyj) - 1;
+            anyj &= anyj - 1u;
+            const int kk = j0 + j;
+            const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
+            const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
+            uint32_t need = __ballot_sync(kFull, (nearm >> j) & 1u);
+            while (need) {
+                const int l = __ffs(need) - 1;
+                need &= need - 1u;
+                const float2* xl = X + (size_t)(n0 + warp * 32 + l) * C;
+                const int s0 = warp_df_diff_sign(xl, xl - C, dh, dl, C, lane);
+                const int s1 = warp_df_diff_sign(xl + C, xl, dh, dl, C, lane);
+                if (lane == l) {
+                    const uint32_t bit = 1u << j;
+                    mxm = (s0 > 0 && s1 < 0) ? (mxm | bit) : (mxm & ~bit);
+                    mnm = (s0 < 0 && s1 > 0) ? (mnm | bit) : (mnm & ~bit);
                 }
             }
-            const uint32_t wmax = __ballot_sync(kFull, inrange && (endpt || (interior && mxf)));
-            const uint32_t wmin = __ballot_sync(kFull, inrange && (endpt || (interior && mnf)));
+        }
+        // the bitmask words: lane j keeps the ballot of direction j0 + j
+        uint32_t my_max = 0u, my_min = 0u;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const uint32_t wmax = __ballot_sync(kFull, inrange && (endpt || (interior && ((mxm >> j) & 1u))));
+            const uint32_t wmin = __ballot_sync(kFull, inrange && (endpt || (interior && ((mnm >> j) & 1u))));
             if (lane == j) {
                 my_max = wmax;
                 my_min = wmin;

@@ -406,7 +406,7 @@ def run_ours(args):
         pipe = "f64" if name == "fp64" else "f32"
         achieved = f / per_launch_s / 1e12
         tr = traffic.get(f"{name}:{dom}")
-        kern = {"project": "k_project_mx" if name.startswith("mixed") else "k_project_extrema",
+        kern = {"project": "k_split_tf32 + k_project_tc" if name.startswith("mixed") else "k_project_extrema",
                 "eval": {"mixed": "k_mean_cum", "mixed_direct": "k_eval_w", "fp32": "k_eval_w", "fp64": "k_eval"}[name],
                 "solve": "k_solve_fwd + k_solve_bwd", "factor": "k_factor", "compact": "k_compact"}[dom]
         step_s = results[name]["ms_per_step"] / 1e3

@@ -410,7 +410,7 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
                                                                         (Fac<R>*)p->fac, g, k0, kc, p->Sf, p->Hf,
                                                                         p->cum ? p->cumcfg : nullptr, p->ep, p->cum_ctas);
         lc.end(MEMD_STAGE_FACTOR);
-        const long nseg = (p->H < 0) ? 1 : (g.cap + p->Ss - 1) / p->Ss;
+        const long nseg = solve_segments_max(g.cap, p->S, p->Ss, p->H);
         const long ns = 2L * kc * nseg * p->ngroups * 32;
         const unsigned nb = (unsigned)((ns + kSolveThreads - 1) / kSolveThreads);
         unsigned* bcur = p->cum ? p->bnd + (size_t)(p->bpass & 1) * 2 * g.C : nullptr;
@@ -1114,6 +1114,16 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
     }
     p->GS = 32;  // solve: one warp per (envelope, direction, segment, 32 channels)
     p->ngroups = (C + 31) / 32;
+    {
+        // the factorisation and substitution kernels index their threads in 32 bits
+        const double nfac = 2.0 * p->Kc * (double)((p->g.cap + p->Sf - 1) / p->Sf);
+        const double nsol = 2.0 * p->Kc * (double)solve_segments_max(p->g.cap, p->S, p->Ss, p->H) * p->ngroups * 32.0;
+        if (nfac >= 2147483648.0 || nsol >= 2147483648.0) {
+            delete p;
+            return set_error(MEMD_ERR_UNSUPPORTED, "plan: a factorisation or substitution launch would exceed 2^31 "
+                                                   "threads (fewer directions per chunk or longer segments)");
+        }
+    }
     // FP64 evaluation tile: G channels x T samples, enough CTAs to fill the GPU
     p->evalG = std::min(32, std::max(4, next_pow2(C)));
     {

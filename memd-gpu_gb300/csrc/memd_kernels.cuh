@@ -413,13 +413,17 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             cumcfg[1] = P;
         }
     }
-    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int nseg = (g.cap + Sf - 1) / Sf;
-    const int seg = (int)(gid % nseg);
-    const long rest = gid / nseg;
-    const int kk = (int)(rest % Kc);
-    const int env = (int)(rest / Kc);
-    if (env >= 2) return;
+    // thread = (segment, envelope, direction), the segment slowest so that
+    // whole CTAs past the systems' knots exit at once; 32-bit index
+    // arithmetic (the plan keeps the launch below 2^31 threads)
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nsys = 2u * (unsigned)Kc;
+    const unsigned segu = gid / nsys;
+    if (segu >= (unsigned)((g.cap + Sf - 1) / Sf)) return;
+    const int seg = (int)segu;
+    const int sys = (int)(gid - segu * nsys);
+    const int env = sys >= Kc ? 1 : 0;
+    const int kk = sys - env * Kc;
     const int E = cnt[env * g.K + k0 + kk];
     if (E > g.cap) return;
     const int i0 = seg * Sf;
@@ -435,6 +439,10 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
     constexpr int FB = 8;  // knot positions loaded per batch (independent loads)
     // FULL (compile-time): all FB rows are owned (>= i0, < i1) and have a right
     // neighbour, so no row needs a guard
+    // A batch in two phases: first every row's coefficients (small integers:
+    // spacings, end conditions) and the reciprocal spacing of its right piece,
+    // none of which depends on the pivots, so their loads and tests overlap;
+    // then the pivot recurrence itself, the only serial part.
     auto batch = [&](auto full, int base) {
         constexpr bool FULL = decltype(full)::value;
         int xs[FB];
@@ -443,47 +451,57 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             const int i = base + k;
             xs[k] = (FULL || (i < i1 && i < E - 1)) ? x[i + 1] : 0;
         }
+        int li[FB], di[FB], ui[FB];
+        [[maybe_unused]] int wn[FB], wd[FB];  // not-a-knot rows: right-hand side weighted by wn / wd (wd > 0)
+        real rt[FB];
+#pragma unroll
+        for (int k = 0; k < FB; ++k) {
+            const int i = base + k;
+            const bool act = FULL || i < i1;
+            const int xr = (FULL || i < E - 1) ? xs[k] : xi;
+            const bool end = record_end_knot(ep, xi, i, E);  // natural end conditions: s = 0
+            const int hl = xi - xl, hr = xr - xi;
+            li[k] = end ? 0 : hl;
+            ui[k] = end ? 0 : hr;
+            di[k] = end ? 1 : 2 * (hl + hr);
+            if constexpr (NAK) {
+                wn[k] = 0;
+                wd[k] = 0;
+                if (!end && E >= 4 && i == 1) {
+                    // s_0 eliminated by the not-a-knot condition d_0 = d_1
+                    li[k] = 0; di[k] = hl + 2 * hr; ui[k] = hr - hl;
+                    wn[k] = hr; wd[k] = hl + hr;
+                } else if (!end && E >= 4 && i == E - 2) {
+                    // s_{E-1} eliminated by d_{E-3} = d_{E-2}
+                    li[k] = hl - hr; di[k] = 2 * hl + hr; ui[k] = 0;
+                    wn[k] = hl; wd[k] = hl + hr;
+                }
+            }
+            rt[k] = (act && (FULL || i < E - 1)) ? rtab[xr - xi] : real(0);
+            if (act) {
+                xl = xi;
+                xi = xr;
+            }
+        }
 #pragma unroll
         for (int k = 0; k < FB; ++k) {
             const int i = base + k;
             if (FULL || i < i1) {
-                const int xr = (FULL || i < E - 1) ? xs[k] : xi;
-                real l, d, u;
-                bool wrow = false;  // a not-a-knot row: right-hand side weighted by wn / wd
-                int wn = 0, wd = 1;
-                if (record_end_knot(ep, xi, i, E)) {  // natural end conditions: s = 0
-                    l = real(0); d = real(1); u = real(0);
-                } else {
-                    const int hl = xi - xl, hr = xr - xi;
-                    l = real(hl); u = real(hr); d = real(2 * (hl + hr));
-                    if constexpr (NAK) {
-                        if (E >= 4 && i == 1) {
-                            // s_0 eliminated by the not-a-knot condition d_0 = d_1
-                            l = real(0); d = real(hl + 2 * hr); u = real(hr - hl);
-                            wrow = true; wn = hr; wd = hl + hr;
-                        } else if (E >= 4 && i == E - 2) {
-                            // s_{E-1} eliminated by d_{E-3} = d_{E-2}
-                            l = real(hl - hr); d = real(2 * hl + hr); u = real(0);
-                            wrow = true; wn = hl; wd = hl + hr;
-                        }
-                    }
-                }
-                const real gp = fmad_(-l, cp, d);
+                const real l = real(li[k]);
+                const real gp = fmad_(-l, cp, real(di[k]));
                 const real m = recip_(gp);
-                cp = mul_(u, m);
+                cp = mul_(real(ui[k]), m);
                 if (FULL || i >= i0) {
                     Fac<real> o;
                     o.m = m;
                     if constexpr (NAK) {
-                        if (wrow) o.m = mul_(m, div_(real(wn), real(wd)));
+                        if (wd[k] > 0) o.m = mul_(m, div_(real(wn[k]), real(wd[k])));
                     }
                     o.lm = mul_(l, m);
                     o.cp = cp;
-                    o.ih = (FULL || i < E - 1) ? fac_ih(rtab[xr - xi]) : real(0);
+                    o.ih = (FULL || i < E - 1) ? fac_ih(rt[k]) : real(0);
                     f[i] = o;
                 }
-                xl = xi;
-                xi = xr;
             }
         }
     };
@@ -536,6 +554,22 @@ __device__ __forceinline__ int solve_seg_len(int E, int cap, int S, int Ss, int 
     return Ss;
 }
 
+// The most segments solve_seg_len gives a system of at most cap knots (the
+// static grid's segment rows): systems of E in (16 t, hi] knots take segments
+// of t, hi the smaller bound left by the longer segments, the rest take Ss.
+__host__ __device__ inline long solve_segments_max(int cap, int S, int Ss, int H)
+{
+    if (H < 0) return 1;
+    long m = 0;
+    int hi = cap;
+    for (int t = S; t > Ss; t >>= 1) {
+        if (hi > 16 * t) m = m > (hi + t - 1) / t ? m : (hi + t - 1) / t;
+        hi = hi < 16 * t ? hi : 16 * t;
+    }
+    const long r = (hi + Ss - 1) / Ss;
+    return m > r ? m : r;
+}
+
 // Device work queue of the substitution (optional, memd_tuning.solve_queue):
 // k_solve_queue writes, per pass, the segments before each (envelope,
 // direction) slot; the persistent sweeps take items (segment x channel group)
@@ -571,11 +605,14 @@ __device__ __forceinline__ SolveItem solve_item_of(int env, int kk, int seg, int
 __device__ __forceinline__ SolveItem solve_item(const int* cnt, const Geom& g, int k0, int Kc, int S, int Ss, int H,
                                                 int ngroups)
 {
-    const long gw = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp = item
-    const int cgi = (int)(gw % ngroups);
-    const long item = gw / ngroups;
-    const int slot = (int)(item % (2 * Kc));
-    const int seg = (int)(item / (2 * Kc));
+    // 32-bit index arithmetic: the plan keeps the launch below 2^31 threads
+    const unsigned gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp = item
+    const unsigned ng = (unsigned)ngroups, nsl = 2u * (unsigned)Kc;
+    const unsigned item = ng == 1u ? gw : gw / ng;
+    const int cgi = (int)(gw - item * ng);
+    const unsigned segu = item / nsl;
+    const int slot = (int)(item - segu * nsl);
+    const int seg = (int)segu;
     return solve_item_of(slot / Kc, slot % Kc, seg, cgi, cnt, g, k0, S, Ss, H);
 }
 
@@ -1510,7 +1547,7 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const int wa = w + (ra >> 5), ba = ra & 31;
     const int wend = min(w + mw, g.W);
     // this CTA's share of the (direction, envelope) pairs
-    const int e_lo = (int)((long)prt * 2 * Kc / P), e_hi = (int)((long)(prt + 1) * 2 * Kc / P);
+    const int e_lo = prt * 2 * Kc / P, e_hi = (prt + 1) * 2 * Kc / P;  // 2 Kc <= 2048, P <= 4
 
     dd aA(0.0f, 0.0f), aB(0.0f, 0.0f), aC(0.0f, 0.0f), aD(0.0f, 0.0f);  // anchor coefficients, summed in a fixed order
     for (int base = e_lo; base < e_hi; base += NE) {
@@ -1753,10 +1790,12 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
             const int r = rb0 + k;
             if (r < r1) {
                 // H(n_a + t) = h0 + t h1 + C(t,2) h2 + C(t,3) h3 (Newton's form, any integer t)
-                const long long t = r - ra;
-                const unsigned long long c2 = (unsigned long long)(t * (t - 1) / 2);
-                const unsigned long long c3 = (unsigned long long)(t * (t - 1) * (t - 2) / 6);
-                const unsigned long long val = kq[r * G + cc] + h0 + (unsigned long long)t * h1 + c2 * h2 + c3 * h3;
+                // |t| <= 128: the binomials are exact in 32-bit integers
+                const int t = r - ra;
+                const unsigned long long c2 = (unsigned long long)(long long)(t * (t - 1) / 2);
+                const unsigned long long c3 = (unsigned long long)(long long)(t * (t - 1) * (t - 2) / 6);
+                const unsigned long long val =
+                    kq[r * G + cc] + h0 + (unsigned long long)(long long)t * h1 + c2 * h2 + c3 * h3;
                 dd tot = fix2dd(val, sh);
                 if (bad) tot = dd(__int_as_float(0x7fc00000), 0.0f);
                 const size_t off = (size_t)(p0 + r) * C + c;

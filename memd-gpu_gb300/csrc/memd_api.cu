@@ -364,8 +364,8 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
                 }
                 dim3 tg((unsigned)((g.L + kTcRows - 1) / kTcRows), (unsigned)((kc + p->tc_nt - 1) / p->tc_nt));
                 k_project_tc<<<tg, kTcThreads, tc_smem_bytes(p->tc_nt), s>>>(
-                    p->maps, (const float2*)p->X, (const float*)p->dir, (const float*)p->dir + (size_t)g.K * g.C,
-                    p->bits, g, k0, kc, p->Cp, p->tc_nt, p->st, p->ep);
+                    p->maps, (const float2*)p->X, (const float*)p->dir, p->bits, g, k0, kc, p->Cp, p->tc_nt, p->st,
+                    p->ep);
             } else {
                 k_project_mx<<<pg, 256, p->proj_smem, s>>>((const float2*)p->X, (const float*)p->dir,
                                                            (const float*)p->dir + (size_t)g.K * g.C, p->bits, g, k0, kc,

@@ -11,7 +11,7 @@
 //
 //   k_split_tf32    the first differences of the working signal (double-float
 //                   X[n][c], differenced in double-float, rounded to float)
-//                   and the directions' high words, each split into tf32 "big"
+//                   and the (float32) directions, each split into tf32 "big"
 //                   and "small" parts, v = big + small + r, |r| <= 2^-22 |v|,
 //                   stored [rows][Cp] (Cp = C rounded up to 32, zero padded)
 //   k_project_tc    TMA (cp.async.bulk.tensor, 128-byte swizzle) stages the
@@ -25,15 +25,14 @@
 //                   words by ballot.
 //
 // Certification.  With S = sum_c |dh_c| max|dx_c| over the tile's rows and its
-// halo row (dx the rounded differences, dh / dl the direction's high / low
-// words), the tensor-core D differs from the exact difference of the
-// projections by at most
+// halo row (dx the rounded differences, dh the float32 direction; S summed
+// with upward rounding), the tensor-core D differs from the exact difference
+// of the projections by at most
 //   (4C + 8) 2^-22 S       the dropped small.small and remainder terms
 //                          (3.01 2^-22 |dx||d| per product) and the
 //                          accumulation, counted as 2 ulp of the largest
 //                          partial sum per product and step
 //   + 2^-24 S              the rounding of the differences to float
-//   + sum_c |dl_c| max|dx_c|  the directions' low words
 // (times 1.01).  A sign within that bound of zero is decided again by a
 // double-float dot product of the double-float differences (~2^-44 relative),
 // so the extrema sets are those of the exact projection except at ties closer
@@ -123,16 +122,20 @@ struct TcMaps {
     CUtensorMap xb, xs, db, ds;
 };
 
+// TMEM columns (and padded per-direction array length) of a tile of n
+// directions: a power of two >= 32.
+__host__ __device__ constexpr int tc_cols(int n) { return n <= 32 ? 32 : (n <= 64 ? 64 : (n <= 128 ? 128 : 256)); }
+
 // Shared memory of k_project_tc for N directions per tile (bytes, with the
-// slack for aligning the operand tiles to 1024 bytes).
+// slack for aligning the operand tiles to 1024 bytes): 52.5 KB at N = 64,
+// four CTAs per SM.
 __host__ __device__ constexpr size_t tc_smem_bytes(int n)
 {
     return 1024 + 2 * (size_t)kTcRows * 128 + 2 * (size_t)n * 128  // operand tiles
-           + sizeof(float) * (4 * (size_t)kTcMaxN                  // first rows of the warps [4][N]
-                              + (size_t)kTcMaxN                    // halo row [N]
-                              + 2 * (size_t)kTcMaxN                // bound sums [2][N]
+           + sizeof(float) * (4 * (size_t)tc_cols(n)               // first rows of the warps [4][NP]
+                              + (size_t)tc_cols(n)                 // halo row [NP]
+                              + (size_t)tc_cols(n)                 // bound sums [NP]
                               + 4 * 32 + 32                        // channel maxima
-                              + 2 * (size_t)n * 33                 // direction words of a block [2][N][33]
                               + 32)                                // halo-row differences of a block
            + 64;                                                   // barriers, TMEM address
 }
@@ -142,21 +145,21 @@ __device__ __forceinline__ int dd_sign(dd v) { return v.hi > 0.f ? 1 : (v.hi < 0
 // The sign of sum_c dir[c] (X1[c] - X0[c]) in double-float, computed by the
 // whole warp: lane l takes channels l, l + 32, ... (one coalesced row load
 // per operand), the lanes' double-float partial sums meet in a butterfly of
-// shuffles; every lane returns lane 0's sign.  Each term is the exact
-// two-product of the direction's high word with the double-float difference
-// plus the low word's product, so the sum carries ~2^-44 relative to
+// shuffles; every lane returns lane 0's sign.  The directions are float32
+// (the mixed form's input), so each term is the exact two-product of the
+// direction with the double-float difference's high word plus its product
+// with the low word, and the sum carries ~2^-44 relative to
 // sum |dir| |X1 - X0|.
 __device__ __noinline__ int warp_df_diff_sign(const float2* __restrict__ x1, const float2* __restrict__ x0,
-                                                 const float* __restrict__ dh, const float* __restrict__ dl, int C,
-                                                 int lane)
+                                                 const float* __restrict__ dh, int C, int lane)
 {
     dd acc(0.f, 0.f);
     for (int c = lane; c < C; c += 32) {
         const dd v = xdiff(x1[c], x0[c]);
-        const float a = dh[c], al = dl[c];
+        const float a = dh[c];
         const float p = __fmul_rn(a, v.hi);
         float e = __fmaf_rn(a, v.hi, -p);
-        e = __fmaf_rn(a, v.lo, __fmaf_rn(al, v.hi, e));
+        e = __fmaf_rn(a, v.lo, e);
         acc = acc + dd_renorm(p, e);
     }
 #pragma unroll
@@ -169,8 +172,7 @@ __device__ __noinline__ int warp_df_diff_sign(const float2* __restrict__ x1, con
 // signal tile).
 __global__ void __launch_bounds__(kTcThreads)
 k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, const float* __restrict__ dh_all,
-             const float* __restrict__ dl_all, uint32_t* __restrict__ bits, Geom g, int k0, int Kc, int Cp, int nt,
-             RunState* st, Epochs ep)
+             uint32_t* __restrict__ bits, Geom g, int k0, int Kc, int Cp, int nt, RunState* st, Epochs ep)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // operand tiles at a 1024-byte boundary (the 128-byte swizzle repeats
@@ -181,14 +183,14 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
     float* As = Ab + kTcRows * kTcKB;                        // [128][32] small parts
     float* Bb = As + kTcRows * kTcKB;                        // [nt][32] directions, big
     float* Bs = Bb + nt * kTcKB;                             // [nt][32] directions, small
-    float* first = Bs + nt * kTcKB;                          // [4 warps][kTcMaxN]: D of each warp's lane 0
-    float* halo = first + 4 * kTcMaxN;                       // [kTcMaxN]: D at sample n0 + 128
-    float* thr = halo + kTcMaxN;                             // [2][kTcMaxN]: sum |dh| max|dx|, sum |dl| max|dx|
-    float* cmx = thr + 2 * kTcMaxN;                          // [4][32] per-warp channel maxima
+    const uint32_t ncols = (uint32_t)tc_cols(nt);  // TMEM columns; per-direction arrays padded to this
+    const int NP = (int)ncols;
+    float* first = Bs + nt * kTcKB;                          // [4 warps][NP]: D of each warp's lane 0
+    float* halo = first + 4 * NP;                            // [NP]: D at sample n0 + 128
+    float* thr = halo + NP;                                  // [NP]: sum |dh| max|dx|, then the bound
+    float* cmx = thr + NP;                                   // [4][32] per-warp channel maxima
     float* mx = cmx + 4 * 32;                                // [32] channel maxima of the block
-    float* dhs = mx + 32;                                    // [nt][33] direction high words of the block
-    float* dls = dhs + nt * 33;                              // [nt][33] low words
-    float* xd = dls + nt * 33;                               // [32] halo-row differences of the block
+    float* xd = mx + 32;                                     // [32] halo-row differences of the block
     uint64_t* bars = reinterpret_cast<uint64_t*>(xd + 32);   // [0] TMA, [1] MMA
     uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bars + 2);
 
@@ -197,7 +199,6 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
     const int n0 = blockIdx.x * kTcRows;
     const int kt0 = blockIdx.y * nt;            // first direction of the tile within the chunk
     const int nk = min(nt, Kc - kt0);           // valid directions of the tile
-    const uint32_t ncols = nt <= 32 ? 32u : (nt <= 64 ? 64u : (nt <= 128 ? 128u : 256u));
     const int nkb = Cp / kTcKB;
     const int nh = n0 + kTcRows;                // the halo row
     const bool has_halo = nh < g.L;
@@ -211,9 +212,12 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         mbar_init(&bars[1], 1);
         fence_mbar_init();
     }
-    for (int i = tid; i < nt; i += kTcThreads) {
+    // halo: D at sample n0 + 128 in FP32 from the rounded differences (the
+    // same numbers the tensor cores see), its error within the same bound;
+    // halo and bound summed over the channel blocks below
+    for (int i = tid; i < NP; i += kTcThreads) {
         thr[i] = 0.f;
-        thr[kTcMaxN + i] = 0.f;
+        halo[i] = 0.f;
     }
     tc_fence_before();
     __syncthreads();
@@ -229,10 +233,6 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         tma_load_2d(Bb, &maps.db, &bars[0], 0, k0 + kt0);
         tma_load_2d(Bs, &maps.ds, &bars[0], 0, k0 + kt0);
     }
-    // halo: D at sample n0 + 128 in FP32 from the rounded differences (the
-    // same numbers the tensor cores see), its error within the same bound;
-    // summed over the channel blocks below
-    for (int kk = tid; kk < nt; kk += kTcThreads) halo[kk] = 0.f;
 
     int fail = 0, kb = 0;  // fail: 1 = a copy, 2 = the products did not complete in time
     for (; kb < nkb; ++kb) {
@@ -243,14 +243,7 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
             tma_load_2d(Bb, &maps.db, &bars[0], kb * kTcKB, k0 + kt0);
             tma_load_2d(Bs, &maps.ds, &bars[0], kb * kTcKB, k0 + kt0);
         }
-        // this block's direction words and halo-row differences into shared
-        // memory (coalesced, while the copies land)
-        for (int i = tid; i < nt * kTcKB; i += kTcThreads) {
-            const int kk = i >> 5, c = kb * kTcKB + (i & 31);
-            const bool ok = kk < nk && c < C;
-            dhs[kk * 33 + (i & 31)] = ok ? dh_all[(size_t)(k0 + kt0 + kk) * C + c] : 0.f;
-            dls[kk * 33 + (i & 31)] = ok ? dl_all[(size_t)(k0 + kt0 + kk) * C + c] : 0.f;
-        }
+        // the halo row's differences of this block (while the copies land)
         if (tid < 32) {
             const int c = kb * kTcKB + tid;
             xd[tid] = (has_halo && c < C) ? xdiff(X[(size_t)nh * C + c], X[(size_t)(nh - 1) * C + c]).hi : 0.f;
@@ -292,20 +285,39 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
             mx[lane] = fmaxf(m, fabsf(xd[lane])) * 1.0009765625f;
         }
         __syncthreads();
-        // this block's part of the halo row and of the bound sums
-        for (int kk = tid; kk < nk; kk += kTcThreads) {
-            const float* dh = dhs + kk * 33;
-            const float* dl = dls + kk * 33;
-            float h = halo[kk], sh = thr[kk], sl = thr[kTcMaxN + kk];
-            const int nc = min(kTcKB, C - kb * kTcKB);
-            for (int c = 0; c < nc; ++c) {
-                h = __fmaf_rn(dh[c], xd[c], h);
-                sh = __fmaf_ru(fabsf(dh[c]), mx[c], sh);
-                sl = __fmaf_ru(fabsf(dl[c]), mx[c], sl);
+        // this block's part of the halo row and of the bound sum, per
+        // direction: warp w takes directions w, w + 4, ...; lane = channel, so
+        // each direction is one coalesced 128-byte row of the direction set
+        // (L1/L2-resident), reduced by shuffles (the bound rounded up)
+        {
+            const int c = kb * kTcKB + lane;
+            const bool cin = c < C;
+            const float xdl = xd[lane], mxl = mx[lane];
+            const float* drow = dh_all + (size_t)(k0 + kt0) * C + (cin ? c : 0);
+            constexpr int DB = 4;  // directions per batch of loads
+            for (int kb0 = warp; kb0 < nk; kb0 += 4 * DB) {
+                float dv[DB];
+#pragma unroll
+                for (int u = 0; u < DB; ++u) {
+                    const int kk = kb0 + 4 * u;
+                    dv[u] = (cin && kk < nk) ? __ldg(drow + (size_t)kk * C) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < DB; ++u) {
+                    const int kk = kb0 + 4 * u;
+                    float h = __fmul_rn(dv[u], xdl);
+                    float sh = __fmul_ru(fabsf(dv[u]), mxl);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        h = __fadd_rn(h, __shfl_xor_sync(kFull, h, o));
+                        sh = __fadd_ru(sh, __shfl_xor_sync(kFull, sh, o));
+                    }
+                    if (lane == 0 && kk < nk) {
+                        halo[kk] = __fadd_rn(halo[kk], h);
+                        thr[kk] = __fadd_ru(thr[kk], sh);
+                    }
+                }
             }
-            halo[kk] = h;
-            thr[kk] = sh;
-            thr[kTcMaxN + kk] = sl;
         }
         const bool done = mbar_wait_bounded(&bars[1], (uint32_t)(kb & 1), kTcWaitClocks);
         tc_fence_after();
@@ -332,7 +344,7 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
     {
         const float eps = (float)(4 * C + 8) * 2.384185791e-7f + 5.9604645e-8f;  // (4C + 8) 2^-22 + 2^-24
         for (int kk = tid; kk < nk; kk += kTcThreads)
-            thr[kk] = 1.01f * __fmaf_ru(eps, thr[kk], thr[kTcMaxN + kk] * 1.0000002f);
+            thr[kk] = 1.01f * __fmul_ru(eps, thr[kk]);
     }
     // pass 1: every warp publishes its lane 0 (its first sample) for the warp before
     const uint32_t tl = taddr + ((uint32_t)(warp * 32) << 16);
@@ -342,7 +354,7 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
         __syncwarp();  // tcgen05.ld is warp-collective
         tmem_ld32(tl + (uint32_t)j0, v);
         if (lane == 0) {
-            float* e = first + warp * kTcMaxN + j0;
+            float* e = first + warp * NP + j0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) e[j] = v[j];
         }
@@ -365,7 +377,7 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
             const int kk = j0 + j;
             const float d0 = v[j];  // D[n]
             float d1 = __shfl_down_sync(kFull, d0, 1);
-            if (lane == 31) d1 = warp == 3 ? halo[kk] : first[(warp + 1) * kTcMaxN + kk];
+            if (lane == 31) d1 = warp == 3 ? halo[kk] : first[(warp + 1) * NP + kk];
             if (d0 > 0.f && d1 < 0.f) mxm |= 1u << j;
             if (d0 < 0.f && d1 > 0.f) mnm |= 1u << j;
             if (interior && kk < nk) {
@@ -382,14 +394,13 @@ k_project_tc(const __grid_constant__ TcMaps maps, const float2* __restrict__ X, 
             anyj &= anyj - 1u;
             const int kk = j0 + j;
             const float* dh = dh_all + (size_t)(k0 + kt0 + kk) * C;
-            const float* dl = dl_all + (size_t)(k0 + kt0 + kk) * C;
             uint32_t need = __ballot_sync(kFull, (nearm >> j) & 1u);
             while (need) {
                 const int l = __ffs(need) - 1;
                 need &= need - 1u;
                 const float2* xl = X + (size_t)(n0 + warp * 32 + l) * C;
-                const int s0 = warp_df_diff_sign(xl, xl - C, dh, dl, C, lane);
-                const int s1 = warp_df_diff_sign(xl + C, xl, dh, dl, C, lane);
+                const int s0 = warp_df_diff_sign(xl, xl - C, dh, C, lane);
+                const int s1 = warp_df_diff_sign(xl + C, xl, dh, C, lane);
                 if (lane == l) {
                     const uint32_t bit = 1u << j;
                     mxm = (s0 > 0 && s1 < 0) ? (mxm | bit) : (mxm & ~bit);

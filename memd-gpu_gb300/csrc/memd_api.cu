@@ -432,8 +432,10 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         if constexpr (P == MEMD_PREC_MIXED) {
             if (p->cum) {  // knot values from the working signal (the impulse-accumulation path)
                 xm = true;
-                if (p->ep.n > 0) MEMD_FWD(true, true, false);  // batched runs: natural ends only
-                else if (g.nak) MEMD_FWD(true, false, true);
+                if (p->ep.n > 0) {  // batched runs: record ends found by position
+                    if (g.nak) MEMD_FWD(true, true, true);
+                    else MEMD_FWD(true, true, false);
+                } else if (g.nak) MEMD_FWD(true, false, true);
                 else MEMD_FWD(true, false, false);
             }
         }
@@ -444,7 +446,10 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
 #undef MEMD_FWD
         lc.end(MEMD_STAGE_SOLVE);
         lc.begin(MEMD_STAGE_SOLVE);
-        if (g.nak)
+        // not-a-knot ends: applied in the sweep for one record, by k_nak_ends
+        // per record for a batch (the sweep then keeps the identity end rows)
+        const bool nak_ends = g.nak && p->ep.n > 0;
+        if (g.nak && !nak_ends)
             k_solve_bwd<R, true><<<p->squeue ? persistent_grid(k_solve_bwd<R, true>, kSolveThreads, p->sms, nb) : nb,
                                    kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
                                                           (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
@@ -455,6 +460,14 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
                                                            (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
                                                            p->knots, q);
         lc.end(MEMD_STAGE_SOLVE);
+        if (nak_ends) {
+            const long nt = 2L * kc * p->ep.n * g.C;
+            lc.begin(MEMD_STAGE_SOLVE);
+            k_nak_ends<R><<<(unsigned)((nt + 127) / 128), 128, 0, s>>>(p->knots, p->cnt, p->wpref,
+                                                                        (const Fac<R>*)p->fac, (R*)p->sv, g, k0, kc,
+                                                                        p->ep, bcur);
+            lc.end(MEMD_STAGE_SOLVE);
+        }
         lc.begin(MEMD_STAGE_EVAL);
         launch_eval<P>(p, s, k0, kc, ch == 0, ch == p->nchunks - 1);
         lc.end(MEMD_STAGE_EVAL);
@@ -1052,8 +1065,8 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
     if (c.boundary != MEMD_BOUNDARY_REFERENCE && c.boundary != MEMD_BOUNDARY_MIRROR)
         return set_error(MEMD_ERR_INVALID, "plan: bad boundary");
     if (c.projection != 0 && c.projection != 1) return set_error(MEMD_ERR_INVALID, "plan: projection must be 0 or 1");
-    if (c.max_epochs > 0 && (c.spline_end != MEMD_SPLINE_NATURAL || c.boundary != MEMD_BOUNDARY_REFERENCE))
-        return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for natural splines and the reference boundary");
+    if (c.max_epochs > 0 && c.boundary != MEMD_BOUNDARY_REFERENCE)
+        return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the reference boundary");
     if (c.max_epochs > 0) {
         if (c.precision == MEMD_PREC_F32)
             return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the FP64 and mixed forms");

@@ -210,6 +210,13 @@ __device__ __forceinline__ bool record_end_knot(const Epochs& ep, int x, int i, 
     const int o = ep.off[e];
     return x == o || x == o + ep.len[e] - 1;
 }
+// First and last sample of the record (epoch) holding sample x of a batch.
+__device__ __forceinline__ void record_bounds(const Epochs& ep, int x, int& first, int& last)
+{
+    const int e = ep.wep[x >> 5];
+    first = ep.off[e];
+    last = first + ep.len[e] - 1;
+}
 
 // Do both envelopes of direction k have more than 3 knots in epoch e?
 __device__ __forceinline__ bool dir_qualifies(const Geom& g, const Epochs& ep, const int* cnt, int k, int e)

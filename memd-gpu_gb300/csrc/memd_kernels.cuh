@@ -459,7 +459,25 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             const int i = base + k;
             const bool act = FULL || i < i1;
             const int xr = (FULL || i < E - 1) ? xs[k] : xi;
-            const bool end = record_end_knot(ep, xi, i, E);  // natural end conditions: s = 0
+            bool end;  // natural end conditions: s = 0
+            [[maybe_unused]] bool nfirst = false, nlast = false;  // not-a-knot rows: second, second-to-last knot
+            if (!NAK || ep.n == 0) {
+                end = record_end_knot(ep, xi, i, E);
+                if constexpr (NAK) {
+                    nfirst = !end && E >= 4 && i == 1;
+                    nlast = !end && E >= 4 && i == E - 2;
+                }
+            } else {
+                // batched: the record's ends are knots, so knot i is its second
+                // knot when its left neighbour is the record's first sample, and
+                // the record has at least four knots when then its right
+                // neighbour is not the last sample (and the mirror image)
+                int rf, rl;
+                record_bounds(ep, xi, rf, rl);
+                end = xi == rf || xi == rl;
+                nfirst = !end && xl == rf && xr != rl;
+                nlast = !end && xr == rl && xl != rf;
+            }
             const int hl = xi - xl, hr = xr - xi;
             li[k] = end ? 0 : hl;
             ui[k] = end ? 0 : hr;
@@ -467,11 +485,11 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
             if constexpr (NAK) {
                 wn[k] = 0;
                 wd[k] = 0;
-                if (!end && E >= 4 && i == 1) {
+                if (nfirst) {
                     // s_0 eliminated by the not-a-knot condition d_0 = d_1
                     li[k] = 0; di[k] = hl + 2 * hr; ui[k] = hr - hl;
                     wn[k] = hr; wd[k] = hl + hr;
-                } else if (!end && E >= 4 && i == E - 2) {
+                } else if (nlast) {
                     // s_{E-1} eliminated by d_{E-3} = d_{E-2}
                     li[k] = hl - hr; di[k] = 2 * hl + hr; ui[k] = 0;
                     wn[k] = hl; wd[k] = hl + hr;
@@ -920,6 +938,54 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     }
     if (bnd && cok) atomicMax(&bnd[C + it.c], __float_as_uint(spart * 1.01f));
     }  // items
+}
+
+// ---------------------------------------------------------------------------
+// Not-a-knot ends of the records of a batched run.  The factorisation solved
+// each record's first and last knot as identity rows and eliminated them from
+// the record's second and second-to-last rows, so the sweeps give every other
+// row; this kernel sets, per (envelope, direction, record, channel) of a
+// record with at least four knots,
+//     s_b   = s_b+1 + (s_b+1 - s_b+2) h_b / h_b+1          (d_b = d_b+1)
+//     s_e-1 = s_e-2 + (s_e-2 - s_e-3) h_e-2 / h_e-3        (d_e-3 = d_e-2)
+// (b .. e-1 the record's knots, h_i = x_i+1 - x_i) with the single-record
+// backward sweep's arithmetic, and raises the mean's bound bnd[C + c] by the
+// two end pieces as that sweep does.
+// ---------------------------------------------------------------------------
+template <typename real>
+__global__ void __launch_bounds__(128)
+k_nak_ends(const int* __restrict__ knots, const int* __restrict__ cnt, const int* __restrict__ wpref,
+           const Fac<real>* __restrict__ fac, real* __restrict__ sv, Geom g, int k0, int Kc, Epochs ep,
+           unsigned* __restrict__ bnd)
+{
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int C = g.C;
+    const long per_slot = (long)ep.n * C;
+    const int slot = (int)(gid / per_slot);
+    if (slot >= 2 * Kc) return;
+    const long r = gid - (long)slot * per_slot;
+    const int e = (int)(r / C), c = (int)(r - (long)e * C);
+    const int env = slot >= Kc ? 1 : 0, kk = slot - env * Kc;
+    if (cnt[env * g.K + k0 + kk] > g.cap) return;
+    const int* wp = wpref + (size_t)slot * (g.W + 1);
+    const int b = wp[ep.w0[e]], en = wp[ep.w0[e + 1]];  // the record's knots: b .. en - 1
+    if (en - b < 4) return;
+    const int* kn = knots + (size_t)slot * g.cap;
+    real* s = sv + (size_t)slot * g.cap * C + c;
+    const Fac<real>* f = fac + (size_t)slot * g.cap;
+    const real s1 = s[(size_t)(b + 1) * C], s2 = s[(size_t)(b + 2) * C];
+    const real s0 = add_(s1, div_(mul_(sub_(s1, s2), real(kn[b + 1] - kn[b])), real(kn[b + 2] - kn[b + 1])));
+    const real sa = s[(size_t)(en - 3) * C], sb = s[(size_t)(en - 2) * C];
+    const int hb = kn[en - 1] - kn[en - 2];
+    const real sl = add_(sb, div_(mul_(sub_(sb, sa), real(hb)), real(kn[en - 2] - kn[en - 3])));
+    s[(size_t)b * C] = s0;
+    s[(size_t)(en - 1) * C] = sl;
+    if (bnd) {
+        const float ih = magf(f[b].ih);
+        float v = __fdividef((kFacIh3<real> ? 2.25f : 0.25f) * (magf(s0) + magf(s1)), ih * ih);
+        v = fmaxf(v, 0.25f * (magf(sb) + magf(sl)) * (float)hb * (float)hb);
+        atomicMax(&bnd[C + c], __float_as_uint(v * 1.01f));
+    }
 }
 
 // ---------------------------------------------------------------------------

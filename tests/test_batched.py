@@ -69,6 +69,43 @@ def test_batched_f64_equals_single_runs_bitwise(chunk):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("chunk", [0, 5])
+def test_batched_not_a_knot_f64_equals_single_runs_bitwise(chunk):
+    """Not-a-knot ends per record (the second and second-to-last rows of each
+    record in the factorisation, the end extrapolations per record after the
+    sweeps): each epoch equals a single-record not-a-knot run bit for bit
+    (FP64), including records of fewer than four knots (natural ends)."""
+    C, K, nimf, it = 6, 16, 4, 4
+    lengths = [1000, 37, 9, 2049, 4096, 777, 1024]
+    recs, offs = _epochs(C, lengths, seed=90)
+    d = oracle.directions(C, K)
+    kw = dict(dir_chunk=chunk, spline_end=mg.SPLINE_NOT_A_KNOT)
+    got, st = _run_batched(recs, lengths, offs, d, nimf, it, mg.PREC_F64, **kw)
+    assert st.flags in (0, 1)  # 1: an epoch too short for any qualified direction (0/0, as a single run)
+    for rec, g in zip(recs, got):
+        ref = _run_single(rec, d, nimf, it, mg.PREC_F64, **kw)
+        assert np.array_equal(g, ref, equal_nan=True)
+
+
+@pytest.mark.gpu
+def test_batched_not_a_knot_mixed_tracks_fp64():
+    C, K, nimf, it = 8, 24, 5, 5
+    lengths = [3000, 1500, 4100, 2048, 900]
+    recs, offs = _epochs(C, lengths, seed=71)
+    d = oracle.directions(C, K).astype(np.float32).astype(np.float64)
+    recs32 = [r.astype(np.float32) for r in recs]
+    kw = dict(spline_end=mg.SPLINE_NOT_A_KNOT)
+    got, st = _run_batched(recs32, lengths, offs, d, nimf, it, mg.PREC_MIXED, **kw)
+    assert st.flags == 0
+    for rec, g in zip(recs32, got):
+        r64 = _run_single(rec.astype(np.float64), d, nimf, it, mg.PREC_F64, **kw)
+        single = _run_single(rec, d, nimf, it, mg.PREC_MIXED, **kw)
+        for i in range(nimf):
+            assert np.linalg.norm(g[i] - r64[i]) <= 1e-6 * np.linalg.norm(r64[i])
+            assert np.linalg.norm(g[i] - single[i]) <= 1e-6 * np.linalg.norm(single[i])
+
+
+@pytest.mark.gpu
 def test_batched_mixed_matches_single_runs_and_fp64():
     C, K, nimf, it = 8, 24, 5, 5
     lengths = [3000, 1500, 4100, 2048, 900]

@@ -132,7 +132,6 @@ def test_plan_rejects_bad_options_on_host(kw):
 
 
 @pytest.mark.parametrize("kw", [
-    dict(max_epochs=4, spline_end=mg.SPLINE_NOT_A_KNOT),
     dict(max_epochs=4, boundary=mg.BOUNDARY_MIRROR),
     dict(precision=mg.PREC_MIXED, mean_eval=2, boundary=mg.BOUNDARY_MIRROR),
 ])

@@ -242,7 +242,7 @@ memd_status memd_run_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_
 
 /* Batched run launched kernel by kernel without the graph, each kernel timed
  * (per-stage figures, as memd_profile_*).  Synchronises the stream.
- * memd_profile_batched_f32 takes mixed-form plans. */
+ * memd_profile_batched_f32 takes FP32 and mixed-form plans. */
 memd_status memd_profile_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
                                      const int64_t* offsets, const double* d_y, const double* d_dir,
                                      double* d_imfs, void* stream, memd_profile* prof);

@@ -278,11 +278,12 @@ static void launch_eval(memd_plan* p, cudaStream_t s, int k0, int kc, int first,
             k_eval_w<G_, S_, XT, R, true><<<grid, 256, Sh::smem_bytes(true), s>>>(                         \
                 (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
                 (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, (R*)p->M, (R*)p->part,   \
-                p->mir);                                                                                   \
+                p->mir, p->ep);                                                                            \
         else                                                                                               \
             k_eval_w<G_, S_, XT, R, false><<<grid, 256, Sh::smem_bytes(false), s>>>(                       \
                 (XT*)p->X, (R*)p->acc, p->bits, p->wpref, p->knots, p->cnt, (const R*)p->rtab,             \
-                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, nullptr, nullptr, p->mir); \
+                (const R*)p->sv, (const R*)p->yv, g, k0, kc, first, last, p->st, nullptr, nullptr, p->mir,  \
+                p->ep);                                                                                    \
         return;                                                                                            \
     }
         MEMD_EVALW_CASES(MEMD_CASE)
@@ -1068,8 +1069,6 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
     if (c.max_epochs > 0 && c.boundary != MEMD_BOUNDARY_REFERENCE)
         return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the reference boundary");
     if (c.max_epochs > 0) {
-        if (c.precision == MEMD_PREC_F32)
-            return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the FP64 and mixed forms");
         if (c.stop_mode != MEMD_STOP_FIXED)
             return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the fixed mode");
         if (c.precision == MEMD_PREC_MIXED && c.mean_eval == 1)
@@ -1404,7 +1403,10 @@ memd_status memd_profile_batched_f32(memd_plan* plan, int32_t n_epochs, const in
     if (plan->prec == MEMD_PREC_MIXED)
         return profile_batched_impl<MEMD_PREC_MIXED>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream,
                                                      prof);
-    return set_error(MEMD_ERR_PRECISION, "profile_batched_f32: plan is not the mixed form");
+    if (plan->prec == MEMD_PREC_F32)
+        return profile_batched_impl<MEMD_PREC_F32>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream,
+                                                   prof);
+    return set_error(MEMD_ERR_PRECISION, "profile_batched_f32: plan is FP64");
 }
 
 memd_status memd_run_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths, const int64_t* offsets,
@@ -1423,7 +1425,8 @@ memd_status memd_run_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_
     if (!plan) return set_error(MEMD_ERR_INVALID, "run_batched: null plan");
     if (plan->prec == MEMD_PREC_MIXED)
         return run_batched_impl<MEMD_PREC_MIXED>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream, stats);
-    if (plan->prec == MEMD_PREC_F32) return set_error(MEMD_ERR_UNSUPPORTED, "run_batched_f32: FP32 plans are not batched");
+    if (plan->prec == MEMD_PREC_F32)
+        return run_batched_impl<MEMD_PREC_F32>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream, stats);
     return set_error(MEMD_ERR_PRECISION, "run_batched_f32: plan is FP64");
 }
 

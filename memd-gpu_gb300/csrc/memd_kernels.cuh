@@ -1268,9 +1268,11 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
          const int* __restrict__ wpref, const int* __restrict__ knots, const int* __restrict__ cnt,
          const R* __restrict__ rtab, const R* __restrict__ sv, const R* __restrict__ yv, Geom g,
          int k0, int Kc, int first_chunk, int last_chunk, RunState* st, R* __restrict__ M,
-         R* __restrict__ part, const int* __restrict__ mir)
+         R* __restrict__ part, const int* __restrict__ mir, Epochs ep)
 {
     // g.mirror: intervals count the mirrored knots too (mirror_before).
+    // ep.n > 0 (batched): a tile (T | 512) lies in one record; pieces, the
+    // qualified directions and Q are the record's own.
     using Sh = EvalWShape<G, SPL, R>;
     constexpr int T = Sh::T;
     constexpr int MI = Sh::MI;
@@ -1283,7 +1285,10 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
     const int n0 = blockIdx.x * T, cg = blockIdx.y;
     const int c = cg * G + cc;
     const bool cok = c < g.C;
-    const int nl = min(T, g.L - n0);
+    const int rec = ep.n > 0 ? ep.wep[n0 >> 5] : 0;
+    const int rend = ep.n > 0 ? ep.off[rec] + ep.len[rec] : g.L;
+    if (n0 >= rend) return;  // gap between epochs; uniform over the CTA
+    const int nl = min(T, rend - n0);
     const int C = g.C;
     const int w0 = n0 >> 5;
     unsigned char* wb = smem_raw + (size_t)warp * PW;
@@ -1293,7 +1298,7 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
     uint32_t* wd = reinterpret_cast<uint32_t*>(kx + MI + 1);
     if (warp == 0) {
         int q = 0;
-        for (int k = lane; k < g.K; k += 32) q += (cnt[k] > 3 && cnt[g.K + k] > 3) ? 1 : 0;
+        for (int k = lane; k < g.K; k += 32) q += dir_qualifies(g, ep, cnt, k, rec) ? 1 : 0;
         q = warp_sum(q);
         if (lane == 0) sQ = q;
     }
@@ -1306,13 +1311,14 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
 
     for (int kk = warp; kk < Kc; kk += Sh::WARPS) {
         const int k = k0 + kk;
-        if (!(cnt[k] > 3 && cnt[g.K + k] > 3)) continue;
+        if (!dir_qualifies(g, ep, cnt, k, rec)) continue;
         if (cnt[k] > g.cap || cnt[g.K + k] > g.cap) continue;
         for (int env = 0; env < 2; ++env) {
             const size_t slot = (size_t)env * Kc + kk;
             const int* wp = wpref + slot * (g.W + 1);
             const uint32_t* b = bits + slot * g.W;
             const int cl0 = wp[w0];
+            const int kb = ep.n > 0 ? wp[ep.w0[rec]] : 0;  // the record's first knot
             const uint32_t myw = (lane < NW && w0 + lane < g.W) ? b[w0 + lane] : 0u;
             const int nlast = nl - 1;
             int cnt_last = 0;
@@ -1322,8 +1328,8 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
                 if (32 * q + 32 <= nlast) cnt_last += __popc(w);
                 else if (32 * q < nlast) cnt_last += __popc(w & ((1u << (nlast - 32 * q)) - 1u));
             }
-            int ia = max(cl0 - 1, 0);
-            int ib = max(cl0 + cnt_last - 1, 0);
+            int ia = max(cl0 - 1, kb);
+            int ib = max(cl0 + cnt_last - 1, kb);
             const int Ee = cnt[env * g.K + k];
             int lp0 = INT_MAX, lp1 = INT_MAX, rp0 = INT_MAX, rp1 = INT_MAX;
             if (g.mirror) {
@@ -1356,7 +1362,7 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
             for (int j = 0; j < SPL; ++j) {
                 const int t = s_first + j;
                 if (t < nl && cok) {
-                    int iv = max(cl0 + cntb - 1, 0);
+                    int iv = max(cl0 + cntb - 1, kb);
                     if (g.mirror)
                         iv = min(max(mirror_before(n0 + t, lp0, lp1, rp0, rp1) + cl0 + cntb - 1, 0), Ee - 2);
                     const int li = min(iv - ia, m - 1);
@@ -1419,7 +1425,8 @@ k_eval_w(XT* __restrict__ X, R* __restrict__ acc_buf, const uint32_t* __restrict
     if (overflow) atomicOr(&st->flags, 2);
     __syncthreads();
     const int Q = sQ;
-    if (!M && last_chunk && Q == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) atomicOr(&st->flags, 1);
+    if (!M && last_chunk && Q == 0 && (blockIdx.x == 0 || ep.n > 0) && blockIdx.y == 0 && threadIdx.x == 0)
+        atomicOr(&st->flags, 1);
     for (int idx = threadIdx.x; idx < T * G; idx += blockDim.x) {
         const int t = idx / G, ch = idx - t * G;
         const int cch = cg * G + ch;

@@ -8,8 +8,7 @@ import oracle
 
 
 def test_batched_plan_limits_on_host():
-    for kw in (dict(precision=mg.PREC_F32), dict(precision=mg.PREC_F64, stop_mode=mg.STOP_CRITERION),
-               dict(precision=mg.PREC_MIXED, mean_eval=1)):
+    for kw in (dict(precision=mg.PREC_F64, stop_mode=mg.STOP_CRITERION), dict(precision=mg.PREC_MIXED, mean_eval=1)):
         with pytest.raises(mg.MemdError) as ei:
             mg.Plan(4, 1000, 8, 3, 2, max_epochs=4, **kw)
         assert ei.value.status == mg.MEMD_ERR_UNSUPPORTED
@@ -106,6 +105,24 @@ def test_batched_not_a_knot_mixed_tracks_fp64():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("chunk", [0, 5])
+def test_batched_f32_equals_single_runs_bitwise(chunk):
+    """The FP32 form (the reference's own precision) batched: each epoch's
+    IMFs equal a single-record FP32 run bit for bit, natural and not-a-knot
+    ends."""
+    C, K, nimf, it = 6, 16, 4, 4
+    recs, offs = _epochs(C, LENGTHS, seed=60)
+    recs = [r.astype(np.float32) for r in recs]
+    d = oracle.directions(C, K)
+    for spline in (mg.SPLINE_NATURAL, mg.SPLINE_NOT_A_KNOT):
+        kw = dict(dir_chunk=chunk, spline_end=spline)
+        got, st = _run_batched(recs, LENGTHS, offs, d, nimf, it, mg.PREC_F32, **kw)
+        for rec, g in zip(recs, got):
+            ref = _run_single(rec, d, nimf, it, mg.PREC_F32, **kw)
+            assert np.array_equal(g, ref, equal_nan=True)
+
+
+@pytest.mark.gpu
 def test_batched_mixed_matches_single_runs_and_fp64():
     C, K, nimf, it = 8, 24, 5, 5
     lengths = [3000, 1500, 4100, 2048, 900]
@@ -142,7 +159,7 @@ def test_batched_api_misuse():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", [mg.PREC_F64, mg.PREC_MIXED])
+@pytest.mark.parametrize("prec", [mg.PREC_F64, mg.PREC_F32, mg.PREC_MIXED])
 def test_batched_profile_equals_graph_run(prec):
     """The kernel-by-kernel profiled batched run computes what the graph does."""
     torch = pytest.importorskip("torch")

@@ -1071,8 +1071,6 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
     if (c.max_epochs > 0) {
         if (c.stop_mode != MEMD_STOP_FIXED)
             return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the fixed mode");
-        if (c.precision == MEMD_PREC_MIXED && c.mean_eval == 1)
-            return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched mixed runs use the impulse-accumulation mean");
         if ((int64_t)c.max_epochs * ((c.length + kEpochAlign - 1) / kEpochAlign * kEpochAlign) > (1LL << 28))
             return set_error(MEMD_ERR_INVALID, "plan: max_epochs x length exceeds 2^28 samples");
     }

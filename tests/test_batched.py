@@ -8,7 +8,7 @@ import oracle
 
 
 def test_batched_plan_limits_on_host():
-    for kw in (dict(precision=mg.PREC_F64, stop_mode=mg.STOP_CRITERION), dict(precision=mg.PREC_MIXED, mean_eval=1)):
+    for kw in (dict(precision=mg.PREC_F64, stop_mode=mg.STOP_CRITERION),):
         with pytest.raises(mg.MemdError) as ei:
             mg.Plan(4, 1000, 8, 3, 2, max_epochs=4, **kw)
         assert ei.value.status == mg.MEMD_ERR_UNSUPPORTED
@@ -137,6 +137,23 @@ def test_batched_mixed_matches_single_runs_and_fp64():
         for i in range(nimf):
             assert np.linalg.norm(g[i] - single[i]) <= 1e-6 * np.linalg.norm(single[i])
             assert np.linalg.norm(g[i] - r64[i]) <= 1e-6 * np.linalg.norm(r64[i])
+
+
+@pytest.mark.gpu
+def test_batched_mixed_direct_mean_matches_impulse_accumulation():
+    """The mixed form's direct mean (every envelope at every sample) in a
+    batch: the same IMFs as the impulse-accumulation batch to 1e-6."""
+    C, K, nimf, it = 8, 24, 5, 5
+    lengths = [3000, 1500, 4100, 2048, 900]
+    recs, offs = _epochs(C, lengths, seed=72)
+    d = oracle.directions(C, K).astype(np.float32).astype(np.float64)
+    recs32 = [r.astype(np.float32) for r in recs]
+    a, sa = _run_batched(recs32, lengths, offs, d, nimf, it, mg.PREC_MIXED, mean_eval=1)
+    b, sb = _run_batched(recs32, lengths, offs, d, nimf, it, mg.PREC_MIXED)
+    assert sa.flags == 0 and sb.flags == 0
+    for ga, gb in zip(a, b):
+        for i in range(nimf):
+            assert np.linalg.norm(ga[i] - gb[i]) <= 1e-6 * np.linalg.norm(gb[i])
 
 
 @pytest.mark.gpu

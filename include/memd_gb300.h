@@ -239,6 +239,12 @@ memd_status memd_run_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_
 memd_status memd_run_batched_f32(memd_plan* plan, int32_t n_epochs, const int64_t* lengths,
                                  const int64_t* offsets, const float* d_y, const float* d_dir,
                                  float* d_imfs, void* stream, memd_stats* stats);
+/* Stop mode, batched: after a run of n_epochs epochs (and after its stream
+ * has been synchronised), the IMFs of each epoch (n_imfs[e]; its unused
+ * slots are zero, the residual is in the last slot, as for one record) and,
+ * if sifts is not NULL, the sifts of its IMFs (sifts[64 e + i], i < 64).
+ * Reads device memory synchronously. */
+memd_status memd_batched_counts(const memd_plan* plan, int32_t n_epochs, int32_t* n_imfs, int32_t* sifts);
 
 /* Batched run launched kernel by kernel without the graph, each kernel timed
  * (per-stage figures, as memd_profile_*).  Synchronises the stream.

@@ -94,6 +94,7 @@ struct memd_plan {
     void* M;     // stop mode: mean envelope of the last pass [L][C]
     void* part;  // stop mode: per channel group, direction and sample sum of (U-L)^2
     void* amp;   // stop mode: amplitude statistic [L]
+    void* recstop;  // stop mode, batched: RecStop per record [max_epochs]
     int egroups; // evaluation channel groups
     uint32_t* bits;
     int* wpref;
@@ -477,11 +478,27 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         if (stop) {
             lc.begin(MEMD_STAGE_OTHER);
             k_amp<R><<<(unsigned)((g.L + 255) / 256), 256, 0, s>>>((const R*)p->part, (R*)p->amp, p->cnt, g, k0, kc,
-                                                                 p->egroups, ch == 0);
+                                                                 p->egroups, ch == 0, p->ep);
             lc.end(MEMD_STAGE_OTHER);
         }
     }
-    if (stop) {
+    if (stop && p->batched) {  // every record decides for itself
+        RecStop* rs = (RecStop*)p->recstop;
+        lc.begin(MEMD_STAGE_OTHER);
+        k_rec_q<<<(unsigned)p->ep.n, 32, 0, s>>>(rs, g, p->ep);
+        lc.end(MEMD_STAGE_OTHER);
+        lc.begin(MEMD_STAGE_OTHER);
+        k_stop_stats_b<R><<<(unsigned)std::min<long>((g.L + 255) / 256, 1024), 256, 0, s>>>(
+            (const R*)p->M, (const R*)p->amp, rs, g, p->ep, p->cfg.stop_sd, p->cfg.stop_sd2);
+        lc.end(MEMD_STAGE_OTHER);
+        lc.begin(MEMD_STAGE_OTHER);
+        k_decide_b<<<1, 1024, 0, s>>>(p->st, rs, p->ep, p->cfg.stop_tol, (int)p->cfg.max_iter, h_sift);
+        lc.end(MEMD_STAGE_OTHER);
+        lc.begin(MEMD_STAGE_OTHER);
+        k_apply_b<R, XT><<<(unsigned)std::min<size_t>(((size_t)g.C * g.L + 255) / 256, 4096), 256, 0, s>>>(
+            (XT*)p->X, (const R*)p->M, rs, g, p->ep);
+        lc.end(MEMD_STAGE_OTHER);
+    } else if (stop) {
         const size_t CL = (size_t)g.C * g.L;
         lc.begin(MEMD_STAGE_OTHER);
         k_stop_stats<R><<<(unsigned)std::min<long>((g.L + 255) / 256, 1024), 256, 0, s>>>(
@@ -590,7 +607,10 @@ static memd_status build_graph_stop(memd_plan* p)
         e = cudaStreamBeginCaptureToGraph(p->cap, obody, nullptr, nullptr, 0, mode);
         if (e != cudaSuccess) break;
         cudaMemcpyAsync(p->X, p->run, CL * sizeof(XT), cudaMemcpyDeviceToDevice, p->cap);
-        k_imf_begin<<<1, 32, 0, p->cap>>>(p->st, (int)p->cfg.max_iter, p->trace_dev ? 1 : 0, h_sift);
+        if (p->batched)
+            k_imf_begin_b<<<1, 1024, 0, p->cap>>>((RecStop*)p->recstop, p->ep, h_sift);
+        else
+            k_imf_begin<<<1, 32, 0, p->cap>>>(p->st, (int)p->cfg.max_iter, p->trace_dev ? 1 : 0, h_sift);
         {
             cudaStreamCaptureStatus cs;
             const cudaGraphNode_t* deps = nullptr;
@@ -615,20 +635,29 @@ static memd_status build_graph_stop(memd_plan* p)
         // sift body: one envelope pass + stop test + (conditional) subtraction
         e = cudaStreamBeginCaptureToGraph(p->cap, ibody, nullptr, nullptr, 0, mode);
         if (e != cudaSuccess) break;
-        enqueue_sift<P>(p, p->cap, p->trace_dev, lc, h_sift);
+        enqueue_sift<P>(p, p->cap, p->batched ? nullptr : p->trace_dev, lc, h_sift);
         e = cudaStreamEndCapture(p->cap, &tmp);
         if (e != cudaSuccess) break;
         // IMF body, part 2: write the IMF, update the residual, continue?
         e = cudaStreamBeginCaptureToGraph(p->cap, obody, &inner, nullptr, 1, mode);
         if (e != cudaSuccess) break;
-        k_imf_out_dyn<XT, T><<<tg, tb, 0, p->cap>>>((const XT*)p->X, (T*)p->imf, (XT*)p->run, p->st, g.C, g.L);
-        k_imf_commit<<<1, 32, 0, p->cap>>>(p->st, nimf, h_imf);
+        if (p->batched) {
+            k_imf_out_b<XT, T><<<tg, tb, 0, p->cap>>>((const XT*)p->X, (T*)p->imf, (XT*)p->run,
+                                                       (const RecStop*)p->recstop, p->ep, g.C, g.L);
+            k_imf_commit_b<<<1, 1024, 0, p->cap>>>(p->st, (RecStop*)p->recstop, p->ep, nimf, h_imf);
+        } else {
+            k_imf_out_dyn<XT, T><<<tg, tb, 0, p->cap>>>((const XT*)p->X, (T*)p->imf, (XT*)p->run, p->st, g.C, g.L);
+            k_imf_commit<<<1, 32, 0, p->cap>>>(p->st, nimf, h_imf);
+        }
         e = cudaStreamEndCapture(p->cap, &tmp);
         if (e != cudaSuccess) break;
         // after the IMF loop: unused slots zeroed, residual into the last slot
         e = cudaStreamBeginCaptureToGraph(p->cap, top, &outer, nullptr, 1, mode);
         if (e != cudaSuccess) break;
-        k_zero_unused<T><<<1024, 256, 0, p->cap>>>((T*)p->imf, p->st, nimf, CL);
+        if (p->batched)
+            k_zero_unused_b<T><<<1024, 256, 0, p->cap>>>((T*)p->imf, (const RecStop*)p->recstop, p->ep, nimf, g.C, g.L);
+        else
+            k_zero_unused<T><<<1024, 256, 0, p->cap>>>((T*)p->imf, p->st, nimf, CL);
         k_to_channel_major<XT, T><<<tg, tb, 0, p->cap>>>((const XT*)p->run, (T*)p->imf + (size_t)(nimf - 1) * CL,
                                                          nullptr, g.C, g.L);
         e = cudaStreamEndCapture(p->cap, &tmp);
@@ -854,7 +883,9 @@ static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths,
     cudaStream_t s = (cudaStream_t)stream;
     memd_status st = batched_inputs<P>(p, n, lengths, offsets, d_y, d_dir, d_imfs, s);
     if (st != MEMD_OK) return st;
-    st = build_graph<P>(p);
+    const bool stopm = p->cfg.stop_mode == MEMD_STOP_CRITERION;
+    if (stopm) cudaMemsetAsync(p->recstop, 0, sizeof(RecStop) * (size_t)n, s);
+    st = stopm ? build_graph_stop<P>(p) : build_graph<P>(p);
     if (st != MEMD_OK) return st;
     const Geom& g = p->g;
     const int C = g.C;
@@ -876,9 +907,14 @@ static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths,
         memset(stats, 0, sizeof(*stats));
         stats->elapsed_ms = ms;
         stats->flags = hs.flags | checked_flags();
-        stats->n_imfs = (int)p->cfg.num_imfs - 1;
-        stats->launches = p->graph_launches + 2;
-        for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
+        if (stopm) {  // per-epoch counts: memd_batched_counts
+            stats->n_imfs = hs.n_imfs;
+            stats->launches = p->graph_launches * (int64_t)hs.pad[0] + 3LL * (hs.n_imfs + 1) + 2;
+        } else {
+            stats->n_imfs = (int)p->cfg.num_imfs - 1;
+            stats->launches = p->graph_launches + 2;
+            for (int i = 0; i + 1 < (int)p->cfg.num_imfs && i < 64; ++i) stats->sifts[i] = (int)p->cfg.max_iter;
+        }
         stats->refined = hs.pad[3];
     }
     return MEMD_OK;
@@ -946,6 +982,8 @@ static memd_status profile_batched_impl(memd_plan* p, int n, const int64_t* leng
 {
     using T = typename Prec<P>::T;
     cudaStream_t s = (cudaStream_t)stream;
+    if (p->cfg.stop_mode == MEMD_STOP_CRITERION)
+        return set_error(MEMD_ERR_UNSUPPORTED, "profile_batched: stop mode is profiled per record (memd_profile_*)");
     memd_status st = batched_inputs<P>(p, n, lengths, offsets, d_y, d_dir, d_imfs, s);
     if (st != MEMD_OK) return st;
     memset(prof, 0, sizeof(*prof));
@@ -1069,8 +1107,6 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
     if (c.max_epochs > 0 && c.boundary != MEMD_BOUNDARY_REFERENCE)
         return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the reference boundary");
     if (c.max_epochs > 0) {
-        if (c.stop_mode != MEMD_STOP_FIXED)
-            return set_error(MEMD_ERR_UNSUPPORTED, "plan: batched runs are built for the fixed mode");
         if ((int64_t)c.max_epochs * ((c.length + kEpochAlign - 1) / kEpochAlign * kEpochAlign) > (1LL << 28))
             return set_error(MEMD_ERR_INVALID, "plan: max_epochs x length exceeds 2^28 samples");
     }
@@ -1223,6 +1259,7 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
         ALLOC(p->M, rb * CL);
         ALLOC(p->part, rb * (size_t)p->egroups * Kc * L);
         ALLOC(p->amp, rb * (size_t)L);
+        if (p->batched) ALLOC(p->recstop, sizeof(RecStop) * (size_t)c.max_epochs);
     }
     if (p->batched) {
         const size_t me = (size_t)c.max_epochs;
@@ -1405,6 +1442,25 @@ memd_status memd_profile_batched_f32(memd_plan* plan, int32_t n_epochs, const in
         return profile_batched_impl<MEMD_PREC_F32>(plan, n_epochs, lengths, offsets, d_y, d_dir, d_imfs, stream,
                                                    prof);
     return set_error(MEMD_ERR_PRECISION, "profile_batched_f32: plan is FP64");
+}
+
+memd_status memd_batched_counts(const memd_plan* plan, int32_t n_epochs, int32_t* n_imfs, int32_t* sifts)
+{
+    using namespace memd;
+    if (!plan || !n_imfs) return set_error(MEMD_ERR_INVALID, "batched_counts: null argument");
+    if (!plan->batched || plan->cfg.stop_mode != MEMD_STOP_CRITERION || !plan->recstop)
+        return set_error(MEMD_ERR_UNSUPPORTED, "batched_counts: the plan is not a batched stop-mode plan");
+    if (n_epochs < 1 || n_epochs > plan->ep.n)
+        return set_error(MEMD_ERR_INVALID, "batched_counts: n_epochs exceeds the last run's epochs");
+    std::vector<RecStop> h((size_t)n_epochs);
+    const cudaError_t e = cudaMemcpy(h.data(), plan->recstop, sizeof(RecStop) * h.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return set_cuda_error("batched_counts: read", e);
+    for (int i = 0; i < n_epochs; ++i) {
+        n_imfs[i] = h[i].n_imfs;
+        if (sifts)
+            for (int j = 0; j < 64; ++j) sifts[64 * (size_t)i + j] = j < h[i].n_imfs ? h[i].sifts[j] : 0;
+    }
+    return MEMD_OK;
 }
 
 memd_status memd_run_batched_f64(memd_plan* plan, int32_t n_epochs, const int64_t* lengths, const int64_t* offsets,

@@ -267,6 +267,23 @@ struct RunState {
                                // [3] extremum tests re-decided in double-float
 };
 
+// Stop mode, batched runs: the decision state of one record (epoch); the
+// fields of RunState that belong to a single record, per record.
+struct RecStop {
+    int nbit;      // sifts applied to the record's current IMF
+    int pass;      // envelope passes of the current IMF
+    int imf_done;  // the record's residual has too few extrema (its decomposition ends)
+    int fin;       // the record's decomposition has ended (no further IMF)
+    int apply;     // subtract the mean of the last pass from this record
+    int sifting;   // the record takes part in the current sift loop
+    int n_imfs;    // IMFs written for the record
+    int q;         // qualified directions of the last pass
+    int few;       // every direction has fewer than 3 interior extrema (last pass)
+    int pad;
+    unsigned long long over1, over2;  // samples with sigma > sd, > sd2 in the last pass
+    int sifts[64];                    // sifts per IMF
+};
+
 __device__ __forceinline__ uint64_t splitmix64(uint64_t z)
 {
     z += 0x9E3779B97F4A7C15ull;

@@ -2268,13 +2268,14 @@ k_mirror(const uint32_t* __restrict__ bits, const XT* __restrict__ X, const real
 
 template <typename real>
 __global__ void k_amp(const real* __restrict__ part, real* __restrict__ amp, const int* __restrict__ cnt,
-                      Geom g, int k0, int Kc, int groups, int first_chunk)
+                      Geom g, int k0, int Kc, int groups, int first_chunk, Epochs ep)
 {
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < g.L; n += gridDim.x * blockDim.x) {
         real a = first_chunk ? real(0) : amp[n];
+        const int rec = ep.n > 0 ? ep.wep[n >> 5] : 0;  // qualification of the sample's record
         for (int kk = 0; kk < Kc; ++kk) {
             const int k = k0 + kk;
-            if (!(cnt[k] > 3 && cnt[g.K + k] > 3)) continue;
+            if (!dir_qualifies(g, ep, cnt, k, rec)) continue;
             real s2 = real(0);
             for (int q = 0; q < groups; ++q) s2 = add_(s2, part[((size_t)q * Kc + kk) * g.L + n]);
             a = fmad_(sqrt_(s2), real(0.5), a);
@@ -2445,6 +2446,215 @@ __global__ void k_zero_unused(real* __restrict__ imf, const RunState* __restrict
     const size_t begin = (size_t)st->n_imfs * CL, end = (size_t)(nimf - 1) * CL;
     for (size_t i = begin + (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < end; i += (size_t)gridDim.x * blockDim.x)
         imf[i] = real(0);
+}
+
+// ---------------------------------------------------------------------------
+// Stop mode, batched runs: every record (epoch) takes its own decisions, with
+// the single-record rules (k_decide, k_imf_commit) applied to its own counts,
+// length and statistics; the graph's sift and IMF loops run while any record
+// goes on, and a record that has stopped is neither updated nor written
+// again.  Gap samples between records are never read or written.
+// ---------------------------------------------------------------------------
+// Per record: qualified directions and whether every direction has fewer
+// than 3 interior extrema (one warp per record).
+__global__ void k_rec_q(RecStop* __restrict__ rs, Geom g, Epochs ep)
+{
+    const int e = blockIdx.x, lane = threadIdx.x;
+    if (e >= ep.n) return;
+    int q = 0;
+    bool few = true;
+    for (int k = lane; k < g.K; k += 32) {
+        const int a = ep.cnt[(size_t)k * ep.n + e], b = ep.cnt[((size_t)g.K + k) * ep.n + e];
+        if (a > 3 && b > 3) ++q;
+        if ((a - 2) + (b - 2) >= 3) few = false;  // interior extrema: the knots less the two end samples
+    }
+    q = warp_sum(q);
+    few = __all_sync(kFull, few);
+    if (lane == 0) {
+        rs[e].q = q;
+        rs[e].few = few ? 1 : 0;
+    }
+}
+
+// sigma statistics per record: a warp's 32 consecutive samples are one
+// bitmask word, which lies in one record.
+template <typename real>
+__global__ void __launch_bounds__(256)
+k_stop_stats_b(const real* __restrict__ M, const real* __restrict__ amp, RecStop* __restrict__ rs, Geom g, Epochs ep,
+               double sd, double sd2)
+{
+    const int lane = threadIdx.x & 31;
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long nw = (long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); nw < g.L; nw += stride) {
+        const int n = (int)nw + lane;
+        const int e = ep.wep[nw >> 5];  // the word's record (uniform over the warp)
+        if (!rs[e].sifting) continue;
+        const bool in = n < g.L && n - ep.off[e] < ep.len[e];
+        bool o1 = false, o2 = false;
+        if (in) {
+            real m2 = real(0);
+            for (int c = 0; c < g.C; ++c) {
+                const real v = M[(size_t)n * g.C + c];
+                m2 = fmad_(v, v, m2);
+            }
+            const real a = div_(amp[n], real(rs[e].q));
+            real sig;
+            if (a > real(0.0f)) sig = div_(sqrt_(m2), a);
+            else sig = m2 > real(0.0f) ? real(INFINITY) : real(0.0f);
+            o1 = static_cast<double>(sig) > sd;
+            o2 = static_cast<double>(sig) > sd2;
+        }
+        const unsigned b1 = __ballot_sync(kFull, o1), b2 = __ballot_sync(kFull, o2);
+        if (lane == 0) {
+            if (b1) atomicAdd(&rs[e].over1, (unsigned long long)__popc(b1));
+            if (b2) atomicAdd(&rs[e].over2, (unsigned long long)__popc(b2));
+        }
+    }
+}
+
+// One CTA: the stop test of every sifting record; the sift loop goes on
+// while any record does.
+__global__ void __launch_bounds__(1024)
+k_decide_b(RunState* st, RecStop* __restrict__ rs, Epochs ep, double tol, int max_iter,
+           cudaGraphConditionalHandle h_sift)
+{
+    int any = 0;
+    for (int e = threadIdx.x; e < ep.n; e += blockDim.x) {
+        RecStop& r = rs[e];
+        r.apply = 0;
+        if (!r.sifting) continue;
+        int cont = 0;
+        if (r.pass == 0 && r.few) {
+            r.imf_done = 1;
+        } else {
+            const bool stop = (r.q == 0) || !(((double)r.over1 / (double)ep.len[e] > tol) || r.over2 > 0);
+            if (!stop) {
+                r.apply = 1;
+                r.nbit += 1;
+                cont = r.nbit < max_iter ? 1 : 0;
+            }
+        }
+        r.pass += 1;
+        r.over1 = 0;
+        r.over2 = 0;
+        r.sifting = cont;
+        any |= cont;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        st->pad[0] += 1;
+        st->pad[1] = any;
+        if (h_sift) cudaGraphSetConditional(h_sift, any ? 1u : 0u);
+    }
+}
+
+// X -= M on the samples of the records whose last pass is applied.
+template <typename real, typename XT>
+__global__ void k_apply_b(XT* __restrict__ X, const real* __restrict__ M, const RecStop* __restrict__ rs, Geom g,
+                          Epochs ep)
+{
+    const size_t total = (size_t)g.L * g.C;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int n = (int)(i / g.C);
+        const int e = ep.wep[n >> 5];
+        if (rs[e].apply && n - ep.off[e] < ep.len[e]) X[i] = xsub(X[i], M[i]);
+    }
+}
+
+// One CTA, before each IMF's sift loop: the records still decomposing sift.
+__global__ void __launch_bounds__(1024)
+k_imf_begin_b(RecStop* __restrict__ rs, Epochs ep, cudaGraphConditionalHandle h_sift)
+{
+    int any = 0;
+    for (int e = threadIdx.x; e < ep.n; e += blockDim.x) {
+        RecStop& r = rs[e];
+        r.nbit = 0;
+        r.pass = 0;
+        r.imf_done = 0;
+        r.apply = 0;
+        r.over1 = 0;
+        r.over2 = 0;
+        r.sifting = r.fin ? 0 : 1;
+        any |= r.sifting;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0 && h_sift) cudaGraphSetConditional(h_sift, any ? 1u : 0u);
+}
+
+// The IMF of each record that produced one, into the record's next slot;
+// the running residual updated.  One CTA per (32-sample word, 32 channels).
+template <typename XT, typename TO>
+__global__ void k_imf_out_b(const XT* __restrict__ X, TO* __restrict__ imf, XT* __restrict__ run,
+                            const RecStop* __restrict__ rs, Epochs ep, int C, int L)
+{
+    __shared__ XT tile[32][33];
+    const int n_base = blockIdx.x * 32, c_base = blockIdx.y * 32;
+    const int e = ep.wep[n_base >> 5];  // the word's record
+    if (rs[e].fin || rs[e].imf_done) return;  // uniform over the CTA
+    const int nend = ep.off[e] + ep.len[e];
+    TO* out = imf + (size_t)rs[e].n_imfs * C * L;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int n = n_base + r, c = c_base + threadIdx.x;
+        if (c < C && n < nend) {
+            const size_t idx = (size_t)n * C + c;
+            const XT v = X[idx];
+            tile[r][threadIdx.x] = v;
+            run[idx] = xsub(run[idx], v);
+        }
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        const int c = c_base + r, n = n_base + threadIdx.x;
+        if (c < C && n < nend) out[(size_t)c * L + n] = xfrom<TO>(tile[threadIdx.x][r]);
+    }
+}
+
+// One CTA, after each IMF's sift loop: count the IMFs; the IMF loop goes on
+// while any record does (RunState.n_imfs: the most IMFs of any record).
+__global__ void __launch_bounds__(1024)
+k_imf_commit_b(RunState* st, RecStop* __restrict__ rs, Epochs ep, int nimf, cudaGraphConditionalHandle h_imf)
+{
+    int any = 0, most = 0;
+    for (int e = threadIdx.x; e < ep.n; e += blockDim.x) {
+        RecStop& r = rs[e];
+        if (!r.fin) {
+            if (!r.imf_done) {
+                const int i = r.n_imfs;
+                if (i < 64) r.sifts[i] = r.nbit;
+                r.n_imfs = i + 1;
+                if (r.n_imfs >= nimf - 1) r.fin = 1;
+            } else {
+                r.fin = 1;
+            }
+        }
+        any |= r.fin ? 0 : 1;
+        most = max(most, r.n_imfs);
+    }
+    any = __syncthreads_or(any);
+    __shared__ int smost;
+    if (threadIdx.x == 0) smost = 0;
+    __syncthreads();
+    atomicMax(&smost, most);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->n_imfs = smost;
+        st->pad[2] = any;
+        if (h_imf) cudaGraphSetConditional(h_imf, any ? 1u : 0u);
+    }
+}
+
+// Zero the IMF slots a record left unused.
+template <typename real>
+__global__ void k_zero_unused_b(real* __restrict__ imf, const RecStop* __restrict__ rs, Epochs ep, int nimf, int C,
+                                int L)
+{
+    const size_t CL = (size_t)C * L, total = (size_t)(nimf - 1) * CL;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int s = (int)(i / CL);
+        const int n = (int)(i % (size_t)L);
+        const int e = ep.wep[n >> 5];
+        if (s >= rs[e].n_imfs) imf[i] = real(0);
+    }
 }
 
 // ---------------------------------------------------------------------------

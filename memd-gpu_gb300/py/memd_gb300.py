@@ -43,7 +43,7 @@ EXPORTS = [
     "memd_default_config", "memd_plan_create", "memd_plan_create_tuned", "memd_plan_get_tuning",
     "memd_plan_destroy", "memd_plan_workspace_bytes",
     "memd_plan_set_trace", "memd_run_f64", "memd_run_f32", "memd_run_batched_f64",
-    "memd_run_batched_f32", "memd_profile_f64", "memd_profile_f32", "memd_profile_batched_f64",
+    "memd_run_batched_f32", "memd_batched_counts", "memd_profile_f64", "memd_profile_f32", "memd_profile_batched_f64",
     "memd_profile_batched_f32", "memd_directions_f64", "memd_directions_f32", "memd_directions_noalloc_f64", "memd_diag_fma_rate", "memd_diag_wait_timeout", "memd_last_error",
     "memd_version", "memd_synth_tones", "memd_synth_eeg", "memd_write_bin", "memd_bin_count",
     "memd_read_bin",
@@ -173,6 +173,8 @@ def _load(path):
         f = getattr(L, name)
         f.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Stats)]
         f.restype = ctypes.c_int
+    L.memd_batched_counts.argtypes = [vp, i32, vp, vp]
+    L.memd_batched_counts.restype = ctypes.c_int
     for name in ("memd_profile_f64", "memd_profile_f32"):
         f = getattr(L, name)
         f.argtypes = [vp, vp, vp, vp, vp, ctypes.POINTER(Profile)]
@@ -310,6 +312,17 @@ class Plan:
                   _dptr(dirs), _dptr(imfs), _stream_ptr(stream),
                   ctypes.byref(st) if stats else None))
         return st if stats else None
+
+    def batched_counts(self, n_epochs: int):
+        """Stop mode, batched: (IMFs per epoch, sifts per IMF and epoch [n, 64])
+        of the last run_batched (call after its stream is synchronised)."""
+        import numpy as np
+
+        ni = np.zeros(n_epochs, dtype=np.int32)
+        sf = np.zeros((n_epochs, 64), dtype=np.int32)
+        self._chk(self._L.memd_batched_counts(self.handle, int(n_epochs), ni.ctypes.data_as(ctypes.c_void_p),
+                                              sf.ctypes.data_as(ctypes.c_void_p)))
+        return ni, sf
 
     def profile_batched(self, y, lengths, offsets, dirs, imfs, stream=None) -> Profile:
         """Batched run with every kernel timed by CUDA events (per-stage ms)."""

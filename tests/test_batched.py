@@ -8,10 +8,9 @@ import oracle
 
 
 def test_batched_plan_limits_on_host():
-    for kw in (dict(precision=mg.PREC_F64, stop_mode=mg.STOP_CRITERION),):
-        with pytest.raises(mg.MemdError) as ei:
-            mg.Plan(4, 1000, 8, 3, 2, max_epochs=4, **kw)
-        assert ei.value.status == mg.MEMD_ERR_UNSUPPORTED
+    with pytest.raises(mg.MemdError) as ei:
+        mg.Plan(4, 1000, 8, 3, 2, max_epochs=4, boundary=mg.BOUNDARY_MIRROR)
+    assert ei.value.status == mg.MEMD_ERR_UNSUPPORTED
     with pytest.raises(mg.MemdError) as ei:
         mg.Plan(4, 1 << 20, 8, 3, 2, max_epochs=512)
     assert ei.value.status == mg.MEMD_ERR_INVALID
@@ -228,3 +227,66 @@ def test_batched_two_layouts_on_a_side_stream_without_sync():
     for got, want, offs, lens in ((ga, want_a, oa, la), (gb, want_b, ob, lb)):
         for w, off, L in zip(want, offs, lens):
             assert np.array_equal(got[nimf * off: nimf * off + nimf * C * L].reshape(nimf, C, L), w, equal_nan=True)
+
+
+def _stop_epochs(C, lengths, seed):
+    # tones for some records (few IMFs, short sift loops), EEG-shaped for the others
+    recs = []
+    for e, L in enumerate(lengths):
+        recs.append(mg.synth_tones(C, L, 1000.0, seed=seed + e) if e % 2 else mg.synth_eeg(C, L, 256.0, seed=seed + e))
+    offs = np.concatenate([[0], np.cumsum([C * L for L in lengths])[:-1]]).astype(np.int64)
+    return recs, offs
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [mg.PREC_F64, mg.PREC_F32, mg.PREC_MIXED])
+def test_batched_stop_mode_equals_single_runs(prec):
+    """Stop criterion in a batch: every record sifts and stops by its own
+    statistics, so each epoch has the IMF and sift counts of its single-record
+    stop run and the same IMFs (FP64 and FP32 bit for bit: the arithmetic per
+    record is the same; the mixed form to 1e-6), its unused slots zero and
+    the residual in the last slot."""
+    torch = pytest.importorskip("torch")
+    C, K, nimf, it = 6, 16, 8, 40
+    lengths = [1500, 2600, 900, 37, 4100, 1024]
+    recs, offs = _stop_epochs(C, lengths, seed=300)
+    d = oracle.directions(C, K)
+    tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
+    if prec != mg.PREC_F64:
+        recs = [r.astype(np.float32) for r in recs]
+    kw = dict(precision=prec, stop_mode=mg.STOP_CRITERION)
+    plan = mg.Plan(C, max(lengths), K, nimf, it, max_epochs=len(lengths), **kw)
+    y = torch.as_tensor(np.concatenate([r.ravel() for r in recs]), dtype=tdt, device="cuda")
+    out = torch.full((nimf * y.numel(),), float("nan"), dtype=tdt, device="cuda")
+    st = plan.run_batched(y, lengths, offs, torch.as_tensor(d, dtype=tdt, device="cuda"), out)
+    ni, sf = plan.batched_counts(len(lengths))
+    plan.close()
+    o = out.cpu().numpy()
+    assert st.n_imfs == ni.max()
+    for e, (rec, off, L) in enumerate(zip(recs, offs, lengths)):
+        got = o[nimf * off: nimf * off + nimf * C * L].reshape(nimf, C, L)
+        sp = mg.Plan(C, L, K, nimf, it, **kw)
+        ref = torch.empty((nimf, C, L), dtype=tdt, device="cuda")
+        ss = sp.run(torch.as_tensor(rec, dtype=tdt, device="cuda"), torch.as_tensor(d, dtype=tdt, device="cuda"), ref)
+        sp.close()
+        assert ni[e] == ss.n_imfs, e
+        assert list(sf[e, : ni[e]]) == list(ss.sifts[: ss.n_imfs]), e
+        r = ref.cpu().numpy()
+        if prec != mg.PREC_MIXED:
+            assert np.array_equal(got, r, equal_nan=True), e
+        else:
+            # the double-float sweeps' windows start where the batch's knot
+            # counts put them, so the last bits may differ from a single run
+            for i in range(nimf):
+                n = np.linalg.norm(r[i])
+                assert np.linalg.norm(got[i] - r[i]) <= 1e-6 * max(n, 1e-30), (e, i)
+
+
+@pytest.mark.gpu
+def test_batched_stop_counts_misuse():
+    torch = pytest.importorskip("torch")
+    plan = mg.Plan(4, 500, 8, 3, 2, max_epochs=2)  # fixed mode
+    with pytest.raises(mg.MemdError) as ei:
+        plan.batched_counts(2)
+    assert ei.value.status == mg.MEMD_ERR_UNSUPPORTED
+    plan.close()

@@ -1148,7 +1148,9 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
         p->Hf = -1;
     } else {
         // halo lengths: the truncation error decays by <= 1/2 (solve) and
-        // <= 1/3 (pivots) per knot; FP64 and double-float need ~1e-15
+        // <= 1/12 (pivots: u l / (2 (l + u) - l cp)^2 with cp <= 1/2) per
+        // knot; FP64 and double-float need ~1e-15 (double-float pivots: 16
+        // rows, 12^-16 = 5e-18)
         const bool wide = f64 || c.precision == MEMD_PREC_MIXED;
         p->S = tu.solve_segment ? tu.solve_segment : 256;
         p->Ss = tu.solve_min_segment ? tu.solve_min_segment : std::min(64, p->S);
@@ -1156,7 +1158,7 @@ memd_status memd_plan_create_tuned(const memd_config* cfg, const memd_tuning* tu
         // short factorisation segments (the pivot recurrence is latency-bound),
         // except for FP64, whose longer halo would dominate
         p->Sf = tu.factor_segment ? tu.factor_segment : (f64 ? 64 : 16);
-        p->Hf = f64 ? 40 : (wide ? 32 : 20);
+        p->Hf = f64 ? 40 : (wide ? 16 : 20);
     }
     p->GS = 32;  // solve: one warp per (envelope, direction, segment, 32 channels)
     p->ngroups = (C + 31) / 32;

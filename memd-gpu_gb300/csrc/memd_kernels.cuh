@@ -370,7 +370,9 @@ k_compact(const uint32_t* __restrict__ bits, int* __restrict__ wpref, int* __res
 // Channel-independent factorisation.  One thread per (envelope, direction,
 // segment of Sf rows); the pivot recurrence starts Hf rows early (exact when
 // the window reaches row 0, whose pivot is 1 with cp = 0; otherwise the
-// start error decays by at least 1/3 per row).  rtab[h] = 1/h.
+// start error decays by a factor u l / (2 (l + u) - l cp)^2 <= 1/12 per row,
+// cp <= 1/2, l and u the row's neighbouring spacings; identity and
+// not-a-knot end rows restart it).  rtab[h] = 1/h.
 // ---------------------------------------------------------------------------
 template <typename real, bool NAK>
 __global__ void __launch_bounds__(128)

@@ -107,7 +107,9 @@ typedef struct {
     int32_t ref_window;    /* 1: extrema tested only at interior samples
                               n <= 240*ceil(L/242), as the reference's launch
                               (memReducedEpochs_dev.cu:1191-1195) does; 0: all */
-    int32_t dir_chunk;     /* directions per pass (0 = all K at once) */
+    int32_t dir_chunk;     /* directions per pass (0 = automatic: as many of the K as fit in 60% of
+                              the device's free memory at plan creation; a plan whose allocation
+                              still fails is made again with half as many) */
     int32_t solve_window;  /* tridiagonal halo in knots (0 = default; <0 = exact) */
     int32_t max_epochs;    /* batched runs: epochs per call (0 = single record) */
     int32_t mean_eval;     /* mean envelope: 0 = automatic (impulse accumulation

@@ -192,7 +192,11 @@ typedef struct {
                                    128 .. 65536 (2048) */
     int32_t proj_tile_n;        /* tensor-core projection: directions per tile, a multiple of 16 in
                                    [16, 256] (64) */
-    int32_t reserved[10];
+    int32_t solve_layout;       /* substitution storage: 1 = the solution overwrites the eliminated
+                                   right-hand side (one array, halo rows copied aside), 2 = separate
+                                   arrays, 0 = separate while every direction of the pass fits in the
+                                   memory budget, in place when that fits more (same results) */
+    int32_t reserved[9];
 } memd_tuning;
 
 void memd_default_config(memd_config* cfg);

@@ -95,6 +95,9 @@ struct memd_plan {
     void* part;  // stop mode: per channel group, direction and sample sum of (U-L)^2
     void* amp;   // stop mode: amplitude statistic [L]
     void* recstop;  // stop mode, batched: RecStop per record [max_epochs]
+    void* hz;       // in-place substitution: the first H rows of every segment [2][Kc][hsegs][H][C]
+    int hsegs;      // segments per slot at most (solve_segments_max)
+    int inplace;    // the backward sweep writes the solution over dbuf (dbuf == sv)
     int egroups; // evaluation channel groups
     uint32_t* bits;
     int* wpref;
@@ -189,7 +192,8 @@ static bool make_tile_map(CUtensorMap* m, void* base, uint64_t cols, uint64_t ro
 // buffers once.  Fewer passes re-run the projection, compaction and mean over
 // the record fewer times (512 batched epochs of 32 x 1024..8192 samples, 64
 // directions: three passes 1.80 s, one pass 1.31 s).
-static int directions_that_fit(const memd_config& c, const Geom& g, int rb, int xbytes, int tbytes, bool cum)
+static int directions_that_fit(const memd_config& c, const Geom& g, int rb, int xbytes, int tbytes, bool cum,
+                               bool inplace)
 {
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || fr == 0) {
@@ -198,7 +202,11 @@ static int directions_that_fit(const memd_config& c, const Geom& g, int rb, int 
     }
     const double C = g.C, L = g.L, cap = g.cap, W = g.W;
     const bool stop = c.stop_mode == MEMD_STOP_CRITERION;
-    const double per_dir = 2.0 * cap * (4.0 + 4.0 * rb + (double)rb * C * (cum ? 2.0 : 3.0)) + 8.0 * (2.0 * W + 1.0) +
+    // eliminated right-hand sides and solutions (one array in place, with a
+    // quarter for the halo copies at most), knot values unless the mean reads
+    // the signal
+    const double arrays = (inplace ? 1.25 : 2.0) + (cum ? 0.0 : 1.0);
+    const double per_dir = 2.0 * cap * (4.0 + 4.0 * rb + (double)rb * C * arrays) + 8.0 * (2.0 * W + 1.0) +
                            (stop ? (double)rb * std::ceil(C / 4.0) * L : 0.0);
     const double fixed = C * L * (3.0 * xbytes + (double)tbytes * (double)c.num_imfs + 2.0 * rb) + 8.0 * 39.0 * W * C +
                          8.0 * (C + 31.0) * L + 24.0 * (double)c.directions * C;
@@ -454,7 +462,8 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
                                                                       kSolveThreads, p->sms, nb) : nb,          \
                                           kSolveThreads, 0, s>>>(                                              \
         (const R*)p->yv, p->cnt, (const Fac<R>*)p->fac, (R*)p->dbuf, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, \
-        bcur, XM_ ? (const XT*)p->X : nullptr, p->knots, XM_ ? (const R*)p->yend : nullptr, p->ep, q)
+        bcur, XM_ ? (const XT*)p->X : nullptr, p->knots, XM_ ? (const R*)p->yend : nullptr, p->ep,               \
+        p->inplace ? (R*)p->hz : nullptr, p->hsegs, q)
         if constexpr (P == MEMD_PREC_MIXED) {
             if (p->cum) {  // knot values from the working signal (the impulse-accumulation path)
                 xm = true;
@@ -475,16 +484,21 @@ static void enqueue_sift(memd_plan* p, cudaStream_t s, memd_trace_entry* trace, 
         // not-a-knot ends: applied in the sweep for one record, by k_nak_ends
         // per record for a batch (the sweep then keeps the identity end rows)
         const bool nak_ends = g.nak && p->ep.n > 0;
-        if (g.nak && !nak_ends)
-            k_solve_bwd<R, true><<<p->squeue ? persistent_grid(k_solve_bwd<R, true>, kSolveThreads, p->sms, nb) : nb,
-                                   kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
-                                                          (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
-                                                          p->knots, q);
+        if (g.nak && !nak_ends)  // one record: never in place (its sweep writes the last row from another warp)
+            k_solve_bwd<R, true, false>
+                <<<p->squeue ? persistent_grid(k_solve_bwd<R, true, false>, kSolveThreads, p->sms, nb) : nb,
+                   kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0, kc,
+                                          p->S, p->Ss, p->H, p->ngroups, bcur, p->knots, nullptr, 0, q);
+        else if (p->inplace)
+            k_solve_bwd<R, false, true>
+                <<<p->squeue ? persistent_grid(k_solve_bwd<R, false, true>, kSolveThreads, p->sms, nb) : nb,
+                   kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, nullptr, (R*)p->sv, g, k0, kc, p->S,
+                                          p->Ss, p->H, p->ngroups, bcur, p->knots, (const R*)p->hz, p->hsegs, q);
         else
-            k_solve_bwd<R, false><<<p->squeue ? persistent_grid(k_solve_bwd<R, false>, kSolveThreads, p->sms, nb) : nb,
-                                    kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf,
-                                                           (R*)p->sv, g, k0, kc, p->S, p->Ss, p->H, p->ngroups, bcur,
-                                                           p->knots, q);
+            k_solve_bwd<R, false, false>
+                <<<p->squeue ? persistent_grid(k_solve_bwd<R, false, false>, kSolveThreads, p->sms, nb) : nb,
+                   kSolveThreads, 0, s>>>(p->cnt, (const Fac<R>*)p->fac, (const R*)p->dbuf, (R*)p->sv, g, k0, kc,
+                                          p->S, p->Ss, p->H, p->ngroups, bcur, p->knots, nullptr, 0, q);
         lc.end(MEMD_STAGE_SOLVE);
         if (nak_ends) {
             const long nt = 2L * kc * p->ep.n * g.C;
@@ -1086,6 +1100,7 @@ memd_status memd_plan_get_tuning(const memd_plan* p, memd_tuning* t)
     t->solve_queue = p->squeue ? 1 : 2;
     t->mean_ctas = p->cum_ctas;
     t->proj_tile_n = p->tc ? p->tc_nt : 0;
+    t->solve_layout = p->inplace ? 1 : 2;
     return MEMD_OK;
 }
 
@@ -1132,6 +1147,7 @@ static memd_status create_plan(const memd_config* cfg, const memd_tuning* tun, m
         return set_error(MEMD_ERR_INVALID, "tuning: mean_ctas must be in [128, 65536]");
     if (tu.proj_tile_n && (tu.proj_tile_n % 16 != 0 || tu.proj_tile_n < 16 || tu.proj_tile_n > kTcMaxN))
         return set_error(MEMD_ERR_INVALID, "tuning: proj_tile_n must be a multiple of 16 in [16, 256]");
+    if (tu.solve_layout < 0 || tu.solve_layout > 2) return set_error(MEMD_ERR_INVALID, "tuning: solve_layout must be 0, 1 or 2");
     *out = nullptr;
     const memd_config c = *cfg;
     if (c.channels < 1 || c.channels > 256) return set_error(MEMD_ERR_INVALID, "plan: channels must be in [1, 256]");
@@ -1179,10 +1195,26 @@ static memd_status create_plan(const memd_config* cfg, const memd_tuning* tun, m
     p->g.nak = c.spline_end == MEMD_SPLINE_NOT_A_KNOT;
     p->g.mirror = c.boundary == MEMD_BOUNDARY_MIRROR;
     p->Kc = (c.dir_chunk > 0) ? std::min<int>((int)c.dir_chunk, K) : K;
-    if (c.dir_chunk <= 0) {  // automatic: as many directions per pass as the free memory allows
+    bool want_inplace = tu.solve_layout == 1;
+    if (c.dir_chunk <= 0 && tu.solve_layout == 0) {
+        // automatic: as many directions per pass as the free memory allows,
+        // with separate right-hand-side and solution arrays while all of them
+        // fit (the faster layout), solving in place when that fits more
         const bool cum_cfg = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED &&
                              c.boundary == MEMD_BOUNDARY_REFERENCE && c.mean_eval != 1;
-        const int fit = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg);
+        const int want = std::min(K, kc_limit);
+        const int fit_sep = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, false);
+        if (fit_sep >= want) {
+            p->Kc = want;
+        } else {
+            const int fit_inp = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, true);
+            p->Kc = std::max(1, std::min(want, std::max(fit_sep, fit_inp)));
+            want_inplace = fit_inp > fit_sep;
+        }
+    } else if (c.dir_chunk <= 0) {  // layout fixed by the tuning: the directions that fit with it
+        const bool cum_cfg = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED &&
+                             c.boundary == MEMD_BOUNDARY_REFERENCE && c.mean_eval != 1;
+        const int fit = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, want_inplace);
         p->Kc = std::max(1, std::min({K, fit, kc_limit}));
     }
     *kc_used = p->Kc;
@@ -1293,7 +1325,20 @@ static memd_status create_plan(const memd_config* cfg, const memd_tuning* tun, m
     if (!p->cum) ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
     else ALLOC(p->yend, rb * 2 * Kc * (size_t)std::max<int64_t>(1, c.max_epochs) * 2 * C);  // [2][Kc][epochs][2][C]
     ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
-    ALLOC(p->dbuf, rb * 2 * Kc * p->g.cap * C);
+    // in place (when memory limits the directions per pass): the solution
+    // overwrites the eliminated right-hand side row by row (same warp, read
+    // first); the halo rows a warp reads from the next segment are copied
+    // aside by the forward sweep.  Not for one record with not-a-knot ends,
+    // whose backward sweep writes the last row from another segment's warp
+    // (batched runs set their ends after the sweep).
+    p->inplace = want_inplace && (p->H < 0 || p->Ss >= p->H) && !(p->g.nak && !p->batched);
+    p->hsegs = p->H > 0 ? (int)solve_segments_max(p->g.cap, p->S, p->Ss, p->H) : 0;
+    if (p->inplace) {
+        p->dbuf = p->sv;
+        if (p->H > 0) ALLOC(p->hz, rb * 2 * Kc * (size_t)p->hsegs * p->H * C);
+    } else {
+        ALLOC(p->dbuf, rb * 2 * Kc * p->g.cap * C);
+    }
     // longest knot gap: a record (epoch) length; mirrored knots reach 2L - 2
     const int Lh = p->batched ? std::max(p->Lrec, kEpochAlign) : (p->g.mirror ? 2 * L : L);
     ALLOC(p->rtab, rb * (size_t)(Lh + 1));

@@ -536,10 +536,14 @@ k_factor(const int* __restrict__ knots, const int* __restrict__ cnt, const real*
 // segment, group of 32 channels); each lane one channel (lanes past the last
 // channel compute on a copy of it and store nothing).
 //   k_solve_fwd: forward sweep over [i0-H, i1), writing the eliminated right
-//                -hand side d of rows [i0, i1) to dbuf;
+//                -hand side d of rows [i0, i1) to dbuf (and, in place, its
+//                first H rows also to hz);
 //   k_solve_bwd: backward sweep from i1+H-1 down to i0, reading d of the
-//                segment and of the next segment's first H rows from dbuf,
-//                writing the solution of rows [i0, i1) to sv.
+//                segment and of the next segment's first H rows from dbuf
+//                (in place: the latter from hz), writing the solution of rows
+//                [i0, i1) to sv.  In place dbuf == sv: each warp reads a row's
+//                d before it writes that row's solution, and no other warp
+//                reads the row, so one [2][Kc][cap][C] array serves both.
 // Rows go in batches of 8: every lane loads its 8 values at once, lanes
 // 0..7 load the batch's factor rows, which the sweep takes by shuffle, so a
 // batch costs one memory round trip instead of one per row.
@@ -729,8 +733,12 @@ __global__ void __launch_bounds__(kSolveThreads)
 k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<real>* __restrict__ fac,
             real* __restrict__ dbuf, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
             unsigned* __restrict__ bnd, const XT* __restrict__ X, const int* __restrict__ knots,
-            const real* __restrict__ yend, Epochs ep, SolveQueue q)
+            const real* __restrict__ yend, Epochs ep, real* __restrict__ hz, int hsegs, SolveQueue q)
 {
+    // hz != nullptr (the backward sweep solves in place in dbuf): the first H
+    // rows of every segment also go to hz[slot][segment][H][C], the halo the
+    // backward sweep of the segment before reads while this one's rows are
+    // being overwritten by their solutions
     // XM: knot values read from the working signal, y_i = X[x_i] (interior
     // knots) and yend (the clamped end knots of each record), instead of yv;
     // EPB (with XM): batched epochs, a record's end knots found by position.
@@ -854,15 +862,26 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
         if (i1 < E) ymax = fmaxf(ymax, magf(yi));  // right end of the last piece
         atomicMax(&bnd[it.c], __float_as_uint(ymax * 1.01f));
     }
+    if (hz && cok && i0 > 0 && MEMD_CHECK(it.seg < hsegs)) {  // the halo of the segment before, set aside
+        real* hs = hz + (((size_t)slot * hsegs + it.seg) * H) * C + cl;
+        const int nh = min(H, i1 - i0);
+        for (int r = 0; r < nh; ++r) hs[(size_t)r * C] = o[(size_t)(i0 + r) * C];
+    }
     }  // items
 }
 
-template <typename real, bool NAK>
+template <typename real, bool NAK, bool INPL>
 __global__ void __launch_bounds__(kSolveThreads)
 k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, const real* __restrict__ dbuf,
             real* __restrict__ sv, Geom g, int k0, int Kc, int S, int Ss, int H, int ngroups,
-            unsigned* __restrict__ bnd, const int* __restrict__ knots, SolveQueue q)
+            unsigned* __restrict__ bnd, const int* __restrict__ knots, const real* __restrict__ hz, int hsegs,
+            SolveQueue q)
 {
+    // INPL (dbuf unused): the eliminated right-hand side is in sv,
+    // each row's read by the same warp just before it writes the row's
+    // solution there; the next segment's first H rows (the halo) come from
+    // hz, copied there by the forward sweep, since that segment's own warp
+    // overwrites them.
     // NAK (not-a-knot end conditions, g.nak), E >= 4: rows 0 and E-1 were solved as
     // identity rows; s_0 = s_1 + (h_0 / h_1)(s_1 - s_2) is applied at row 0,
     // and s_{E-1} = s_{E-2} + (h_{E-2} / h_{E-3})(s_{E-2} - s_{E-3}) by the
@@ -879,10 +898,14 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
     const int cl = min(it.c, C - 1);
     const size_t slot = (size_t)it.env * Kc + it.kk;
     const Fac<real>* f = fac + slot * g.cap;
-    const real* d = dbuf + slot * (size_t)g.cap * C + cl;
+    const real* d = (INPL ? sv : dbuf) + slot * (size_t)g.cap * C + cl;
     real* o = sv + slot * (size_t)g.cap * C + cl;
     const int* kn = knots + slot * g.cap;
     const bool nak = NAK && E >= 4;
+    // the next segment's first rows, as the forward sweep left them
+    const real* hzs = (INPL && hz && i1 < E && MEMD_CHECK(it.seg + 1 < hsegs))
+                          ? hz + (((size_t)slot * hsegs + it.seg + 1) * H) * C + cl
+                          : nullptr;
     const int ie = (H < 0) ? E : min(E, i1 + H);
     real snext = real(0), snext2 = real(0);
     float spart = 0.0f;
@@ -900,7 +923,9 @@ k_solve_bwd(const int* __restrict__ cnt, const Fac<real>* __restrict__ fac, cons
         real db[B];
 #pragma unroll
         for (int k = 0; k < B; ++k)
-            db[k] = ((FULL || k < nb) && MEMD_CHECK(top - k >= 0 && top - k < g.cap)) ? d[(size_t)(top - k) * C] : real(0);
+            db[k] = ((FULL || k < nb) && MEMD_CHECK(top - k >= 0 && top - k < g.cap))
+                        ? ((hzs && top - k >= i1) ? hzs[(size_t)(top - k - i1) * C] : d[(size_t)(top - k) * C])
+                        : real(0);
 #pragma unroll
         for (int k = 0; k < B; ++k) {
             const real cp = shfl_idx_(fcp, k), ihr = shfl_idx_(fih, k);

@@ -89,9 +89,11 @@ class Tuning(ctypes.Structure):
         ("solve_queue", ctypes.c_int32),
         ("mean_ctas", ctypes.c_int32),
         ("proj_tile_n", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 10),
+        ("solve_layout", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 9),
     ]
-    KEYS = ("solve_segment", "solve_min_segment", "factor_segment", "solve_queue", "mean_ctas", "proj_tile_n")
+    KEYS = ("solve_segment", "solve_min_segment", "factor_segment", "solve_queue", "mean_ctas", "proj_tile_n",
+            "solve_layout")
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k in self.KEYS}

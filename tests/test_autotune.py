@@ -43,7 +43,7 @@ def test_store_and_lookup_round_trip(tmp_path, monkeypatch):
 
 @pytest.mark.parametrize("bad", [dict(solve_segment=100), dict(solve_segment=2048), dict(solve_min_segment=512),
                                  dict(factor_segment=2), dict(solve_queue=3), dict(mean_ctas=64),
-                                 dict(proj_tile_n=40), dict(proj_tile_n=512)])
+                                 dict(proj_tile_n=40), dict(proj_tile_n=512), dict(solve_layout=3)])
 def test_out_of_range_launch_shapes_are_rejected(bad):
     with pytest.raises(mg.MemdError) as ei:
         mg.Plan(4, 1000, 8, 3, 2, precision=mg.PREC_MIXED, tuning=bad)
@@ -99,3 +99,50 @@ def test_work_queue_substitution_gives_the_static_results():
             plan.close()
             outs.append(o.cpu().numpy())
         assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.gpu
+def test_in_place_substitution_gives_the_separate_arrays_results():
+    """The solution written over the eliminated right-hand side (the halo
+    rows a warp reads from the next segment copied aside by the forward
+    sweep) computes exactly what separate arrays compute: single records
+    (FP64, mixed with direction chunks, the work queue), batched epochs
+    (mixed, FP64 with not-a-knot ends)."""
+    torch = pytest.importorskip("torch")
+    import oracle
+
+    cases = ((mg.PREC_F64, 6, 5000, 24, {}, {}), (mg.PREC_MIXED, 40, 4000, 20, {}, {}),
+             (mg.PREC_MIXED, 12, 3000, 40, {"dir_chunk": 16}, {}), (mg.PREC_MIXED, 8, 6000, 16, {}, {"solve_queue": 1}),
+             (mg.PREC_F32, 8, 3000, 16, {}, {}))
+    for prec, C, L, K, kw, tun in cases:
+        y = mg.synth_eeg(C, L, 256.0, seed=C + L)
+        d = oracle.directions(C, K)
+        tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
+        outs = []
+        for lay in (2, 1):
+            plan = mg.Plan(C, L, K, 4, 4, precision=prec, tuning=dict(tun, solve_layout=lay), **kw)
+            assert plan.tuning()["solve_layout"] == lay
+            o = torch.empty((4, C, L), dtype=tdt, device="cuda")
+            st = plan.run(torch.as_tensor(y, dtype=tdt, device="cuda"), torch.as_tensor(d, dtype=tdt, device="cuda"), o)
+            assert st.flags == 0
+            plan.close()
+            outs.append(o.cpu().numpy())
+        assert np.array_equal(outs[0], outs[1]), (prec, C, L, K)
+    C, K = 8, 16
+    lengths = np.array([1500, 2600, 900, 4100], dtype=np.int64)
+    recs = [mg.synth_eeg(C, int(n), 256.0, seed=200 + i) for i, n in enumerate(lengths)]
+    offs = np.concatenate([[0], np.cumsum(C * lengths)[:-1]]).astype(np.int64)
+    for prec, kw in ((mg.PREC_MIXED, {}), (mg.PREC_F64, {"spline_end": mg.SPLINE_NOT_A_KNOT})):
+        tdt = torch.float64 if prec == mg.PREC_F64 else torch.float32
+        y = torch.as_tensor(np.concatenate([r.ravel() for r in recs]), dtype=tdt, device="cuda")
+        d = torch.as_tensor(oracle.directions(C, K), dtype=tdt, device="cuda")
+        outs = []
+        for lay in (2, 1):
+            plan = mg.Plan(C, int(lengths.max()), K, 4, 4, precision=prec, max_epochs=4,
+                           tuning={"solve_layout": lay}, **kw)
+            o = torch.empty(4 * y.numel(), dtype=tdt, device="cuda")
+            st = plan.run_batched(y, lengths, offs, d, o)
+            assert st.flags == 0
+            plan.close()
+            outs.append(o.cpu().numpy())
+        assert np.array_equal(outs[0], outs[1]), prec

@@ -1606,10 +1606,22 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     constexpr int NE = 256;  // (direction, envelope) pairs described per round
     constexpr int KB = 4;    // knots per batch of loads
     extern __shared__ __align__(16) unsigned long long kq[];  // [32 * kCumMaxWords + 3][G]: jump of d at row x - p0
-    __shared__ unsigned long long anc[4 * G];
-    __shared__ unsigned long long part[NWS * G];  // per row group: totals of a scan pass
-    __shared__ unsigned long long pst[6 * G];     // particular solution at n_a; look-ahead jumps
-    __shared__ int eI[NE], eJ[NE], eN[NE], eX[NE], eH[NE];
+    // The pairs' descriptions are dead once the pairs are done; the anchor
+    // sums and the scan state live only after that, so the two share one
+    // buffer (less shared memory per CTA leaves more of the SM's L1)
+    union Shared {
+        struct {
+            int I[NE], J[NE], N[NE], X[NE], H[NE];
+        } e;
+        struct {
+            unsigned long long anc[4 * G];
+            unsigned long long part[NWS * G];  // per row group: totals of a scan pass
+            unsigned long long pst[6 * G];     // particular solution at n_a; look-ahead jumps
+        } f;
+    };
+    __shared__ __align__(16) Shared su;
+    int *eI = su.e.I, *eJ = su.e.J, *eN = su.e.N, *eX = su.e.X, *eH = su.e.H;
+    unsigned long long *anc = su.f.anc, *part = su.f.part, *pst = su.f.pst;
     __shared__ int sQ, sLast;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cc = lane % G, sub = lane / G;
@@ -1635,7 +1647,6 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
     const bool cok = c < C;
     const int cl = min(c, C - 1);  // loads of lanes past the last channel stay in bounds
     for (int i = threadIdx.x; i < (nl + 3) * G; i += blockDim.x) kq[i] = 0ull;
-    for (int i = threadIdx.x; i < 4 * G; i += blockDim.x) anc[i] = 0ull;
     // quantum: |sum over the chunk's envelopes| <= 2 Kc B < 2^ex
     const float B = __uint_as_float(bnd[cl]) + __uint_as_float(bnd[C + cl]);
     const bool bad = !(B < INFINITY);
@@ -1767,6 +1778,9 @@ k_mean_cum(const float2* __restrict__ X, float2* __restrict__ Xout, dd* __restri
             }
         }
     }
+    __syncthreads();  // the descriptions are dead: anc takes their place
+    for (int i = threadIdx.x; i < 4 * G; i += blockDim.x) anc[i] = 0ull;
+    __syncthreads();
     atomicAdd(&anc[0 * G + cc], qfix(aA, sh));
     atomicAdd(&anc[1 * G + cc], qfix(aB, sh));
     atomicAdd(&anc[2 * G + cc], qfix(aC, sh));

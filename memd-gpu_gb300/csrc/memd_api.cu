@@ -1194,32 +1194,6 @@ static memd_status create_plan(const memd_config* cfg, const memd_tuning* tun, m
     p->g.cov = c.ref_window ? 240 * ((L + 241) / 242) : L;
     p->g.nak = c.spline_end == MEMD_SPLINE_NOT_A_KNOT;
     p->g.mirror = c.boundary == MEMD_BOUNDARY_MIRROR;
-    p->Kc = (c.dir_chunk > 0) ? std::min<int>((int)c.dir_chunk, K) : K;
-    bool want_inplace = tu.solve_layout == 1;
-    if (c.dir_chunk <= 0 && tu.solve_layout == 0) {
-        // automatic: as many directions per pass as the free memory allows,
-        // with separate right-hand-side and solution arrays while all of them
-        // fit (the faster layout), solving in place when that fits more
-        const bool cum_cfg = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED &&
-                             c.boundary == MEMD_BOUNDARY_REFERENCE && c.mean_eval != 1;
-        const int want = std::min(K, kc_limit);
-        const int fit_sep = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, false);
-        if (fit_sep >= want) {
-            p->Kc = want;
-        } else {
-            const int fit_inp = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, true);
-            p->Kc = std::max(1, std::min(want, std::max(fit_sep, fit_inp)));
-            want_inplace = fit_inp > fit_sep;
-        }
-    } else if (c.dir_chunk <= 0) {  // layout fixed by the tuning: the directions that fit with it
-        const bool cum_cfg = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED &&
-                             c.boundary == MEMD_BOUNDARY_REFERENCE && c.mean_eval != 1;
-        const int fit = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, want_inplace);
-        p->Kc = std::max(1, std::min({K, fit, kc_limit}));
-    }
-    *kc_used = p->Kc;
-    p->Kc = std::min(p->Kc, 1024);
-    p->nchunks = (K + p->Kc - 1) / p->Kc;
     if (c.solve_window < 0) {
         p->S = p->g.cap;
         p->Ss = p->g.cap;
@@ -1240,6 +1214,40 @@ static memd_status create_plan(const memd_config* cfg, const memd_tuning* tun, m
         p->Sf = tu.factor_segment ? tu.factor_segment : (f64 ? 64 : 16);
         p->Hf = f64 ? 40 : (wide ? 16 : 20);
     }
+    // in place (when memory limits the directions per pass): the solution
+    // overwrites the eliminated right-hand side row by row (same warp, read
+    // first); the halo rows a warp reads from the next segment are copied
+    // aside by the forward sweep, so segments must be at least a halo long.
+    // Not for one record with not-a-knot ends, whose backward sweep writes the
+    // last row from another segment's warp (batched runs set their ends after
+    // the sweep).
+    const bool inplace_ok = (p->H < 0 || p->Ss >= p->H) && !(p->g.nak && !p->batched);
+    p->Kc = (c.dir_chunk > 0) ? std::min<int>((int)c.dir_chunk, K) : K;
+    bool want_inplace = tu.solve_layout == 1 && inplace_ok;
+    if (c.dir_chunk <= 0 && tu.solve_layout == 0) {
+        // automatic: as many directions per pass as the free memory allows,
+        // with separate right-hand-side and solution arrays while all of them
+        // fit (the faster layout), solving in place when that fits more
+        const bool cum_cfg = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED &&
+                             c.boundary == MEMD_BOUNDARY_REFERENCE && c.mean_eval != 1;
+        const int want = std::min(K, kc_limit);
+        const int fit_sep = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, false);
+        if (fit_sep >= want || !inplace_ok) {
+            p->Kc = std::max(1, std::min(want, fit_sep));
+        } else {
+            const int fit_inp = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, true);
+            p->Kc = std::max(1, std::min(want, std::max(fit_sep, fit_inp)));
+            want_inplace = fit_inp > fit_sep;
+        }
+    } else if (c.dir_chunk <= 0) {  // layout fixed by the tuning: the directions that fit with it
+        const bool cum_cfg = c.precision == MEMD_PREC_MIXED && c.stop_mode == MEMD_STOP_FIXED &&
+                             c.boundary == MEMD_BOUNDARY_REFERENCE && c.mean_eval != 1;
+        const int fit = directions_that_fit(c, p->g, p->real_bytes, p->xbytes, p->tbytes, cum_cfg, want_inplace);
+        p->Kc = std::max(1, std::min({K, fit, kc_limit}));
+    }
+    p->Kc = std::min(p->Kc, 1024);
+    *kc_used = p->Kc;
+    p->nchunks = (K + p->Kc - 1) / p->Kc;
     p->GS = 32;  // solve: one warp per (envelope, direction, segment, 32 channels)
     p->ngroups = (C + 31) / 32;
     {
@@ -1325,13 +1333,7 @@ static memd_status create_plan(const memd_config* cfg, const memd_tuning* tun, m
     if (!p->cum) ALLOC(p->yv, rb * 2 * Kc * p->g.cap * C);
     else ALLOC(p->yend, rb * 2 * Kc * (size_t)std::max<int64_t>(1, c.max_epochs) * 2 * C);  // [2][Kc][epochs][2][C]
     ALLOC(p->sv, rb * 2 * Kc * p->g.cap * C);
-    // in place (when memory limits the directions per pass): the solution
-    // overwrites the eliminated right-hand side row by row (same warp, read
-    // first); the halo rows a warp reads from the next segment are copied
-    // aside by the forward sweep.  Not for one record with not-a-knot ends,
-    // whose backward sweep writes the last row from another segment's warp
-    // (batched runs set their ends after the sweep).
-    p->inplace = want_inplace && (p->H < 0 || p->Ss >= p->H) && !(p->g.nak && !p->batched);
+    p->inplace = want_inplace;
     p->hsegs = p->H > 0 ? (int)solve_segments_max(p->g.cap, p->S, p->Ss, p->H) : 0;
     if (p->inplace) {
         p->dbuf = p->sv;

@@ -146,3 +146,27 @@ def test_in_place_substitution_gives_the_separate_arrays_results():
             plan.close()
             outs.append(o.cpu().numpy())
         assert np.array_equal(outs[0], outs[1]), prec
+
+
+@pytest.mark.gpu
+def test_in_place_layout_falls_back_where_it_does_not_apply():
+    """Asked for where it cannot run (segments shorter than the substitution's
+    halo; one record with not-a-knot ends), the in-place layout gives way to
+    separate arrays: the plan reports that layout and computes what the
+    default plan computes."""
+    torch = pytest.importorskip("torch")
+    import oracle
+
+    C, L, K = 8, 3000, 16
+    y = torch.as_tensor(mg.synth_eeg(C, L, 256.0, seed=77), dtype=torch.float64, device="cuda")
+    d = torch.as_tensor(oracle.directions(C, K), dtype=torch.float64, device="cuda")
+    for tun, kw in (({"solve_min_segment": 16}, {}), ({}, {"spline_end": mg.SPLINE_NOT_A_KNOT})):
+        outs = []
+        for t in (dict(tun), dict(tun, solve_layout=1)):
+            plan = mg.Plan(C, L, K, 4, 4, precision=mg.PREC_F64, tuning=t, **kw)
+            assert plan.tuning()["solve_layout"] == 2
+            o = torch.empty((4, C, L), dtype=torch.float64, device="cuda")
+            assert plan.run(y, d, o).flags == 0
+            plan.close()
+            outs.append(o.cpu().numpy())
+        assert np.array_equal(outs[0], outs[1]), (tun, kw)

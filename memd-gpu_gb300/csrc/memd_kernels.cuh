@@ -794,8 +794,11 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     float ymax = 0.0f;
     // one batch of B rows; FULL (a compile-time flag): all B rows are owned
     // (>= i0), below i1 and have a right neighbour, so no row needs a guard
-    auto batch = [&](auto full, int base) {
+    // INNER (with FULL, one record): no row of the batch is the record's
+    // first or last knot, so every knot value comes from the signal
+    auto batch = [&](auto full, auto inner, int base) {
         constexpr bool FULL = decltype(full)::value;
+        constexpr bool INNER = FULL && !EPB && decltype(inner)::value;
         const int nb = FULL ? B : min(B, i1 - base);
         real fm = real(0), flm = real(0), fih = real(0);
         int fx = 0, ffl = 0, fe = 0;
@@ -814,6 +817,10 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
 #pragma unroll
             for (int k = 0; k < B; ++k) {
                 const int n = __shfl_sync(0xffffffffu, fx, k);
+                if constexpr (INNER) {
+                    yb[k] = xval<real>(X[(size_t)n * C + cl]);
+                    continue;
+                }
                 int fl, e;
                 if constexpr (EPB) {
                     fl = __shfl_sync(0xffffffffu, ffl, k);
@@ -855,8 +862,15 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
         }
     };
     for (int base = is; base < i1; base += B) {
-        if (base >= i0 && base + B <= i1 && base + B < E) batch(std::true_type{}, base);
-        else batch(std::false_type{}, base);
+        const bool full = base >= i0 && base + B <= i1 && base + B < E;
+        if constexpr (XM && !EPB) {
+            if (full && base + B < E - 1) batch(std::true_type{}, std::true_type{}, base);
+            else if (full) batch(std::true_type{}, std::false_type{}, base);
+            else batch(std::false_type{}, std::false_type{}, base);
+        } else {
+            if (full) batch(std::true_type{}, std::false_type{}, base);
+            else batch(std::false_type{}, std::false_type{}, base);
+        }
     }
     if (bnd && cok) {
         if (i1 < E) ymax = fmaxf(ymax, magf(yi));  // right end of the last piece

@@ -813,7 +813,14 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
             }
         }
         real yb[B];
-        if constexpr (XM) {
+        // batched (EPB): a full batch none of whose knots ends a record (one
+        // vote over the lanes' end flags) reads every value from the signal
+        bool inner_rt = false;
+        if constexpr (FULL && EPB && XM) inner_rt = !__any_sync(0xffffffffu, ffl != 0);
+        if (inner_rt) {
+#pragma unroll
+            for (int k = 0; k < B; ++k) yb[k] = xval<real>(X[(size_t)__shfl_sync(0xffffffffu, fx, k) * C + cl]);
+        } else if constexpr (XM) {
 #pragma unroll
             for (int k = 0; k < B; ++k) {
                 const int n = __shfl_sync(0xffffffffu, fx, k);

@@ -44,9 +44,9 @@ for _sub in ("memd-gpu_gb300/py", "oracle"):
 
 # Small cases: each runs in well under a second on the CPU oracle.
 CASES = [
-    # sinusoid mixture, the configs[0] signal family at reduced size
+    # sinusoid mixture (the 8-channel tone workload's signal family), reduced size
     dict(name="tones_c4_l1000_k8", C=4, L=1000, K=8, nimf=5, max_iter=10, kind="tones", seed=1),
-    # configs[0] shape (8 ch x 2000, 64 directions), reference fixed mode, 4 IMFs
+    # the tone workload's shape (8 ch x 2000, 64 directions), reference fixed mode, 4 IMFs
     dict(name="tones_c8_l2000_k64", C=8, L=2000, K=64, nimf=4, max_iter=10, kind="tones", seed=0),
     # L = 4096: the reference extrema launch skips 14 interior samples
     dict(name="pink_c2_l4096_k16", C=2, L=4096, K=16, nimf=5, max_iter=6, kind="pink", seed=2),

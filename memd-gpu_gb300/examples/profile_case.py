@@ -2,6 +2,8 @@
 
     python memd-gpu_gb300/examples/profile_case.py eeg32 [--precision mixed|f64|f32] [--runs R]
     python memd-gpu_gb300/examples/profile_case.py batched --epochs 8 [--precision mixed|f64]
+    ... --stages   (after the runs: one eager run with every kernel timed by CUDA events,
+                    printed as ms and launches per stage; no profiler needed)
 
 eeg32:   32 channels x 30,504 samples (EEG-shaped, seed 0), 128 directions, 9 slots x 10 sifts.
 batched: N epochs of 32 channels, lengths uniform in [1024, 8192] (seed 1000), 64 directions,
@@ -31,6 +33,8 @@ def main():
     ap.add_argument("--runs", type=int, default=1)
     ap.add_argument("--projection", default="auto", choices=["auto", "cuda-cores"],
                     help="mixed form: tensor-core (auto) or CUDA-core projection")
+    ap.add_argument("--stages", action="store_true",
+                    help="also print the per-stage times of one eager run (CUDA events per kernel)")
     a = ap.parse_args()
     if a.runs < 1:
         ap.error("--runs must be at least 1")
@@ -45,6 +49,7 @@ def main():
         out = torch.empty((9, C, L), dtype=tdt, device="cuda")
         for _ in range(a.runs):
             st = plan.run(y, d, out)
+        prof = plan.profile(y, d, out) if a.stages else None
     else:
         C, K, NI, IT, E = 32, 64, 8, 10, a.epochs
         rng = np.random.default_rng(1000)
@@ -57,8 +62,17 @@ def main():
         out = torch.empty(NI * y.numel(), dtype=tdt, device="cuda")
         for _ in range(a.runs):
             st = plan.run_batched(y, lengths, offs, d, out)
+        prof = plan.profile_batched(y, lengths, offs, d, out) if a.stages else None
     print(f"{a.case} {a.precision}: {st.elapsed_ms:.3f} ms, {st.launches} launches, flags {st.flags}, "
           f"tests re-decided in double-float {st.refined}")
+    if prof is not None:
+        stages = prof.as_dict()
+        total = sum(v["ms"] for v in stages.values())
+        print("| stage | ms | launches | share |")
+        print("|---|---|---|---|")
+        for name, v in stages.items():
+            print(f"| {name} | {v['ms']:.3f} | {v['launches']} | {100.0 * v['ms'] / total:.1f}% |")
+        print(f"| total (eager) | {total:.3f} | {sum(v['launches'] for v in stages.values())} | |")
     plan.close()
 
 

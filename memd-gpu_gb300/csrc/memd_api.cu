@@ -783,6 +783,10 @@ static memd_status run_impl(memd_plan* p, const int32_t* d_x, const typename Pre
     cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
     Launches lc;
     enqueue_inputs<P>(p, d_y, d_dir, s, lc);
+    // the copies and clears above must have been accepted before the graph
+    // runs on the buffers they fill
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error("run: inputs", e);
     cudaEventRecord(p->e0, s);
     nvtxRangePushA("memd_run");
     e = cudaGraphLaunch(p->exec, s);
@@ -909,6 +913,10 @@ static memd_status batched_inputs(memd_plan* p, int n, const int64_t* lengths, c
         Launches lc;
         split_directions(p, s, lc);
     }
+    // the copies and clears above must have been accepted before the graph
+    // runs on the buffers they fill
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_cuda_error("run_batched: inputs", e);
     return MEMD_OK;
 }
 
@@ -922,7 +930,10 @@ static memd_status run_batched_impl(memd_plan* p, int n, const int64_t* lengths,
     memd_status st = batched_inputs<P>(p, n, lengths, offsets, d_y, d_dir, d_imfs, s);
     if (st != MEMD_OK) return st;
     const bool stopm = p->cfg.stop_mode == MEMD_STOP_CRITERION;
-    if (stopm) cudaMemsetAsync(p->recstop, 0, sizeof(RecStop) * (size_t)n, s);
+    if (stopm) {
+        const cudaError_t ez = cudaMemsetAsync(p->recstop, 0, sizeof(RecStop) * (size_t)n, s);
+        if (ez != cudaSuccess) return set_cuda_error("run_batched: clear per-epoch state", ez);
+    }
     st = stopm ? build_graph_stop<P>(p) : build_graph<P>(p);
     if (st != MEMD_OK) return st;
     const Geom& g = p->g;
@@ -976,6 +987,14 @@ static memd_status profile_impl(memd_plan* p, const typename Prec<P>::T* d_y, co
     cudaMemsetAsync(p->st, 0, sizeof(RunState), s);
     dim3 tb(32, 8), tg((unsigned)((g.L + 31) / 32), (unsigned)((g.C + 31) / 32));
     enqueue_inputs<P>(p, d_y, d_dir, s, lc);
+    {
+        const cudaError_t ei = cudaGetLastError();
+        if (ei != cudaSuccess) {
+            cudaEventDestroy(lc.a);
+            cudaEventDestroy(lc.b);
+            return set_cuda_error("profile: inputs", ei);
+        }
+    }
     memd_trace_entry* keep = p->trace_dev;
     p->trace_dev = nullptr;
     if (p->cfg.stop_mode == MEMD_STOP_CRITERION) {
@@ -1006,6 +1025,7 @@ static memd_status profile_impl(memd_plan* p, const typename Prec<P>::T* d_y, co
     p->trace_dev = keep;
     cudaMemcpyAsync(d_imfs, p->imf, sizeof(T) * CL * (size_t)p->cfg.num_imfs, cudaMemcpyDeviceToDevice, s);
     cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
     cudaEventDestroy(lc.a);
     cudaEventDestroy(lc.b);
     if (e != cudaSuccess) return set_cuda_error("profile: run", e);
@@ -1037,6 +1057,7 @@ static memd_status profile_batched_impl(memd_plan* p, int n, const int64_t* leng
     k_batched_out<T><<<1024, 256, 0, s>>>((const T*)p->imf, p->ep_yoff, d_imfs, p->g.C, p->g.L,
                                           (int)p->cfg.num_imfs, p->ep);
     cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
     cudaEventDestroy(lc.a);
     cudaEventDestroy(lc.b);
     if (e != cudaSuccess) return set_cuda_error("profile_batched: run", e);

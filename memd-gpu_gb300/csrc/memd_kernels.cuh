@@ -798,7 +798,7 @@ k_solve_fwd(const real* __restrict__ yv, const int* __restrict__ cnt, const Fac<
     // first or last knot, so every knot value comes from the signal
     auto batch = [&](auto full, auto inner, int base) {
         constexpr bool FULL = decltype(full)::value;
-        constexpr bool INNER = FULL && !EPB && decltype(inner)::value;
+        [[maybe_unused]] constexpr bool INNER = FULL && !EPB && decltype(inner)::value;
         const int nb = FULL ? B : min(B, i1 - base);
         real fm = real(0), flm = real(0), fih = real(0);
         int fx = 0, ffl = 0, fe = 0;
